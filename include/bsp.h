@@ -1,0 +1,219 @@
+/*
+ * bsp.h — C ABI of the GB300 (sm_103a) bitmap SpMM library.
+ *
+ * The operation is C = A·B where A is an M×K 0/1 matrix stored as packed
+ * 32-bit row bitmasks and B is a dense K×N matrix.  Every entry point takes
+ * caller-owned device buffers, an explicit CUDA stream and returns an int
+ * status (0 = BSP_OK, negative = error).  No entry point aborts the process.
+ *
+ * The reference (ZSL98/bitwise_spgemm) has no library API: its kernels are
+ * raw __global__ functions launched from main() on the default stream, with
+ * caller-cudaMalloc'ed buffers and shapes fixed by #defines
+ * (source/src/common.h:15-35).  Each declaration below names the reference
+ * kernel or host function it replaces; shapes and layouts that were
+ * compile-time constants there are runtime parameters here.
+ *
+ * Packed-word layout (shared by every entry point): row r of an M×K bit
+ * matrix occupies Kw = ceil(K/32) consecutive uint32 words; word w holds
+ * columns 32w..32w+31.  With BSP_LSB_FIRST column 32w+i is bit i (the layout
+ * of the benchmark configurations); with BSP_MSB_FIRST it is bit 31-i (the
+ * layout of dense2bitmask, source/src/main.cu:611-621).  Bits past column
+ * K-1 in the last word are zero.  Compute entry points read LSB-first words.
+ */
+#ifndef BSP_H_
+#define BSP_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Same object as cudaStream_t; NULL is the legacy default stream. */
+typedef struct CUstream_st* bsp_stream_t;
+
+/* ---- status codes ------------------------------------------------------ */
+enum bsp_status {
+  BSP_OK = 0,
+  BSP_ERR_INVALID_ARG = -1,   /* null pointer, negative/zero size, bad enum  */
+  BSP_ERR_ALIGNMENT = -2,     /* pointer or leading dimension misaligned     */
+  BSP_ERR_WORKSPACE = -3,     /* workspace missing or smaller than required  */
+  BSP_ERR_UNSUPPORTED = -4,   /* valid but not implemented combination       */
+  BSP_ERR_CUDA = -5,          /* a CUDA runtime call or launch failed        */
+  BSP_ERR_DEVICE_TIMEOUT = -6,/* a bounded device-side wait gave up          */
+  BSP_ERR_ALLOC = -7,         /* device/host allocation failed               */
+  BSP_ERR_CAPACITY = -8,      /* input exceeds a documented size limit       */
+  BSP_ERR_QUEUE = -9,         /* batched work-queue descriptor is corrupt    */
+  BSP_ERR_INTERNAL = -10
+};
+
+/* ---- element types ----------------------------------------------------- */
+enum bsp_dtype {
+  BSP_F32 = 0,
+  BSP_F16 = 1,
+  BSP_BF16 = 2,
+  BSP_I8 = 3,
+  BSP_U8 = 4
+};
+
+enum bsp_bit_order { BSP_LSB_FIRST = 0, BSP_MSB_FIRST = 1 };
+
+/* Human-readable name of a status code (static string). */
+const char* bsp_status_string(int status);
+/* Library version as MAJOR*10000 + MINOR*100 + PATCH. */
+int bsp_version(void);
+/* The cudaError_t of the most recent BSP_ERR_CUDA on this host thread. */
+int bsp_last_cuda_error(void);
+
+/* ======================================================================== */
+/* Packing / format conversion                                              */
+/* ======================================================================== */
+
+/* Dense M×K matrix (row stride ld elements) → packed row masks words[M][Kw].
+ * A bit is set iff the element is nonzero (x != 0: -0.0 counts as zero, NaN
+ * as nonzero).  Replaces dense2bitmask, source/src/main.cu:591-628 (MSB-first,
+ * 32-column tiles, atomicOr per nonzero) — here one warp ballot per word.    */
+int bsp_pack_rows(const void* dense, int dtype, int64_t M, int64_t K,
+                  int64_t ld, uint32_t* words, int bit_order,
+                  bsp_stream_t stream);
+
+/* Dense M×K → column-packed masks words_t[K][ceil(M/32)] (the packed rows of
+ * Aᵀ).  The transposed form of dense2bitmask (source/src/main.cu:591-628),
+ * used by the backward pass.                                                */
+int bsp_pack_cols(const void* dense, int dtype, int64_t M, int64_t K,
+                  int64_t ld, uint32_t* words_t, int bit_order,
+                  bsp_stream_t stream);
+
+/* Packed rows of an M×K bit matrix (LSB-first) → packed rows of its K×M
+ * transpose.  No reference counterpart; the bit-matrix form of the
+ * row→column re-tiling done by csr2tiledcsr, source/src/main.cu:499-588.   */
+int bsp_transpose_bits(const uint32_t* words, int64_t M, int64_t K,
+                       uint32_t* words_t, bsp_stream_t stream);
+
+/* Packed masks → dense 0/1 matrix of dtype (row stride ld).  The scatter of
+ * group2dense, source/src/main.cu:829-850, for a full mask.                  */
+int bsp_unpack_rows(const uint32_t* words, int64_t M, int64_t K, void* dense,
+                    int dtype, int64_t ld, int bit_order, bsp_stream_t stream);
+
+/* Bit-plane split of an 8-bit matrix: plane b (0 ≤ b < planes ≤ 8) gets bit
+ * ((uint8)v >> b) & 1 of every element, packed: words[b][M][Kw].  Replaces
+ * uint8_layout_trans / layout_trans, backup/layout_trans.cu:75-97, which
+ * wrote one int per bit.                                                     */
+int bsp_bitplanes(const uint8_t* values, int64_t M, int64_t K, int64_t ld,
+                  int planes, uint32_t* words, int bit_order,
+                  bsp_stream_t stream);
+
+/* ======================================================================== */
+/* Row grouping (reference-compatible first fit)                            */
+/* ======================================================================== */
+
+/* Grouping of packed rows, one tile per (block of tile_rows rows, 32-column
+ * word).  Tiles are numbered t = rb*Kw + w (rb = row block, w = word), as
+ * bid = blockIdx.y*gridDim.x + blockIdx.x in the reference.  Inside a tile the
+ * rows are visited in ascending order; a zero word joins group 0 without
+ * changing its mask; a nonzero word joins the first group g < max_groups whose
+ * mask it does not intersect (the mask gains its bits); otherwise the row
+ * spills.  Replaces generate_groups_large, source/src/main.cu:50-247, whose
+ * shared-memory atomicCAS race is replaced by this deterministic order.
+ *
+ * Outputs (all device, any of the optional ones may be NULL):
+ *   group_id   [M*Kw]  int32: group of row r in word w, -1 if spilled
+ *                      (reference intent main.cu:124/:156; its overwrite of
+ *                      the -1 at main.cu:184 is not reproduced).
+ *   group_mask [T*max_groups] uint32: OR of the member words.
+ *   group_row  [T*max_groups*32] int32 (optional): local row (0..tile_rows-1)
+ *                      that owns bit position i of group g, -1 if none; bit
+ *                      position i is column 32w+i (LSB-first) — the
+ *                      group_ele_row_idx table of main.cu:115-121/:186-190.
+ *   spill_cnt  [T]     int32 (optional): spilled rows per tile.
+ *   spill_nnz  [T]     int32 (optional): set bits of spilled rows per tile.
+ *   spill_rows [T*tile_rows] int32 (optional): ascending local indices of the
+ *                      spilled rows, -1 padded (spilled_row_hash_table).
+ *   grouped_nnz[1]     int64 (optional): Σ popcount(group_mask) (the nnz
+ *                      counter of main.cu:199-204).
+ * tile_rows ∈ [1, 4096], max_groups ∈ [1, 32].                              */
+int bsp_group_rows(const uint32_t* words, int64_t M, int64_t Kw,
+                   int tile_rows, int max_groups, int32_t* group_id,
+                   uint32_t* group_mask, int32_t* group_row,
+                   int32_t* spill_cnt, int32_t* spill_nnz,
+                   int32_t* spill_rows, int64_t* grouped_nnz,
+                   bsp_stream_t stream);
+
+/* Scatter of grouped values back to a dense matrix: for tile t=(rb,w) and
+ * row r of that tile with group g = group_id[r*Kw+w] ≥ 0, every set bit i of
+ * the row's word copies group_values[(t*max_groups+g)*32+i] into
+ * dense[r*ldd + 32w+i].  Replaces group2dense, source/src/main.cu:829-850
+ * (which used MSB-first bits and fixed SIZE_N / TILE_HEIGHT).               */
+int bsp_group_to_dense(const float* group_values, const int32_t* group_id,
+                       const uint32_t* words, int64_t M, int64_t K,
+                       int tile_rows, int max_groups, float* dense,
+                       int64_t ldd, bsp_stream_t stream);
+
+/* ======================================================================== */
+/* SpMM plans (similarity row grouping for the SpMM schedule)               */
+/* ======================================================================== */
+
+typedef struct bsp_plan bsp_plan;
+
+enum bsp_plan_mode {
+  BSP_PLAN_AUTO = 0,     /* choose from the measured cluster structure      */
+  BSP_PLAN_DIRECT = 1,   /* every row walks its own set bits                */
+  BSP_PLAN_PROTO = 2     /* rows = cluster prototype sum ± delta bits       */
+};
+
+typedef struct bsp_plan_params {
+  int mode;              /* enum bsp_plan_mode                              */
+  int signature_hashes;  /* MinHash functions per row (1..8), 0 = default   */
+  int min_cluster_rows;  /* smallest cluster that gets a prototype, 0 = dflt*/
+  uint32_t seed;         /* MinHash permutation seed                        */
+} bsp_plan_params;
+
+typedef struct bsp_plan_info {
+  int64_t M, K;
+  int64_t nnz;           /* set bits of A                                   */
+  int mode;              /* the mode actually used                          */
+  int64_t n_proto;       /* prototypes (clusters with a prototype)          */
+  int64_t proto_nnz;     /* set bits over all prototypes                    */
+  int64_t delta_nnz;     /* ± delta entries over all prototype rows         */
+  int64_t direct_rows;   /* rows without a prototype                        */
+  int64_t direct_nnz;    /* set bits of those rows                          */
+} bsp_plan_info;
+
+/* Build a plan for A (packed LSB-first words[M][ceil(K/32)]).  Runs grouping
+ * kernels on `stream`, then synchronises it once to size the plan's device
+ * buffers, which the plan owns.  The plan is immutable and may be used from
+ * any stream afterwards.  params may be NULL (defaults).  The similarity
+ * grouping has no counterpart in the reference; its first-fit grouping of
+ * disjoint rows is bsp_group_rows.                                           */
+int bsp_plan_create(const uint32_t* words, int64_t M, int64_t K,
+                    const bsp_plan_params* params, bsp_plan** plan,
+                    bsp_stream_t stream);
+int bsp_plan_destroy(bsp_plan* plan);
+int bsp_plan_get_info(const bsp_plan* plan, bsp_plan_info* info);
+
+/* ======================================================================== */
+/* SpMM                                                                     */
+/* ======================================================================== */
+
+/* Device workspace (bytes) that bsp_spmm needs for this plan and N. */
+int bsp_spmm_workspace(const bsp_plan* plan, int64_t N, size_t* bytes);
+
+/* C[M×N] (FP32, row stride ldc) = A·B, A given by its packed words and,
+ * optionally, a plan built from the same words (NULL = walk every row's set
+ * bits).  B is K×N of b_dtype ∈ {F32, F16, BF16}, row stride ldb elements;
+ * accumulation is FP32, rows with more than 4096 set bits use a compensated
+ * (two-term) sum.  Replaces the 0/1-mask SpMM of uint8_spmm_2d_1d /
+ * indexed_spmm_*, backup/layout_trans.cu:120-171 (one global atomicAdd per
+ * set bit and column) and the bit-serial compute kernel
+ * spgemm_compute_1dthread_tcore_v3, source/src/transform.cuh:2062-2248.
+ * Integer-valued B gives results identical to the reference's sum.        */
+int bsp_spmm(const uint32_t* A_words, int64_t M, int64_t K, const void* B,
+             int b_dtype, int64_t ldb, int64_t N, float* C, int64_t ldc,
+             const bsp_plan* plan, void* workspace, size_t workspace_bytes,
+             bsp_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BSP_H_ */
