@@ -1,0 +1,370 @@
+"""Benchmark of the bitmap SpMM hot path (one JSON line on rank 0).
+
+Workload (default): the clustered plain-FP32 configuration — A 8192×8192
+packed bit rows (64 Bernoulli(0.05) prototypes, each row a prototype copy
+with p=0.002 flips), B 8192×512 FP32 N(0,1), C = A·B in FP32.  A "step" is
+one bitmap-SpMM call over one batch (one B); A's plan (similarity row
+grouping) is built once before the timed region, as the reference builds its
+row groups before its timed compute (source/src/main.cu:2045 vs :2150-2202);
+the plan build time is reported separately and is inside the e2e figure.
+
+Metric: GB/s of compulsory bytes (A packed + B + C) per second.
+Timing: CUDA events on the launching stream around K steps replayed from a
+CUDA graph; the steps rotate over 8 independent (B, C) pairs, 256 MiB in
+total (> the 129 MB L2), so no step finds its inputs in L2.
+
+--impl reference times the reference's CPU path (check()'s dense triple loop,
+backup/bit_wise_gemm.cu:13-32, restated in oracle/) on all host threads.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "bitmap-SpMM GB/s (compulsory bytes A+B+C / time)"
+UNIT = "GB/s"
+ROTATE = 8
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=200)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--e2e-steps", type=int, default=10)
+    p.add_argument("--cpu-seconds", type=float, default=10.0)
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+def dist_setup(args):
+    import torch
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend)
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(ws, x):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_from_profiles():
+    """DRAM bytes per step from the committed ncu summary (line
+    'dram_bytes_per_step: <n>'), or None."""
+    path = os.path.join(ROOT, "profiles", "spmm_clustered_8192x8192x512_f32.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("dram_bytes_per_step:"):
+            try:
+                return int(line.split(":")[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.th = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.th = threading.Thread(target=self._read, daemon=True)
+        self.th.start()
+        time.sleep(0.3)
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 7:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=2)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[3 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def workload():
+    from bitwise_spgemm_gb300 import workloads as W
+    cfg = W.config2()
+    M, K, N = cfg["M"], cfg["K"], cfg["N"]
+    bytes_A = M * ((K + 31) // 32) * 4
+    bytes_B = K * N * 4
+    bytes_C = M * N * 4
+    return cfg, bytes_A + bytes_B + bytes_C, (bytes_A, bytes_B, bytes_C)
+
+
+def cpu_sample_rows(cfg, seconds, threads):
+    """Rows of check()'s dense triple loop that `threads` threads finish in
+    about `seconds` (calibrated on one row per thread)."""
+    import oracle as O
+    from bitwise_spgemm_gb300 import workloads as W
+    Ad = W.unpack_bits(cfg["words"][:threads], cfg["K"]).astype(np.float32)
+    t0 = time.perf_counter()
+    O.dense_check_sum(Ad, cfg["B"], threads=threads)
+    t_par = time.perf_counter() - t0
+    return int(min(cfg["M"], threads * max(1, int(seconds / max(t_par, 1e-6)))))
+
+
+def cpu_reference(cfg, rows, threads):
+    """check()'s triple loop (backup/bit_wise_gemm.cu:13-32, restated in
+    oracle/) on the first `rows` rows, extrapolated to all M rows.  Returns
+    (seconds for all rows, description of the sample)."""
+    import oracle as O
+    from bitwise_spgemm_gb300 import workloads as W
+    M, K = cfg["M"], cfg["K"]
+    Ad = W.unpack_bits(cfg["words"][:rows], K).astype(np.float32)
+    t0 = time.perf_counter()
+    O.dense_check_sum(Ad, cfg["B"], threads=threads)
+    dt = time.perf_counter() - t0
+    return dt * M / rows, ("first %d of %d rows of the dense FP32 triple loop (check(), p ascending) "
+                           "on %d threads; time scaled by %d/%d" % (rows, M, threads, M, rows))
+
+
+def run_reference(args):
+    ws, rank, _ = dist_setup(args)
+    if rank != 0:
+        return
+    cfg, comp_bytes, _ = workload()
+    threads = os.cpu_count() or 1
+    per_step = max(0.3, min(10.0, 90.0 / max(1, args.steps + args.warmup)))
+    rows = cpu_sample_rows(cfg, per_step, threads)
+    vals = []
+    sample = ""
+    for i in range(args.warmup + args.steps):
+        t_full, sample = cpu_reference(cfg, rows, threads)
+        if i >= args.warmup:
+            vals.append(comp_bytes / t_full / 1e9)
+    v = float(np.median(vals))
+    out = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": comp_bytes / (v * 1e9) * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded numpy, clustered-rows generator)",
+           "config": {"workload": "clustered_8192x8192x512_f32", "M": 8192, "K": 8192, "N": 512},
+           "impl": "reference",
+           "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                            "sample": sample},
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def run_ours(args):
+    import torch
+    from bitwise_spgemm_gb300 import capi, ops
+    ws, rank, local = dist_setup(args)
+    cfg, comp_bytes, (bA, bB, bC) = workload()
+    M, K, N = cfg["M"], cfg["K"], cfg["N"]
+    words_np = np.ascontiguousarray(cfg["words"]).view(np.int32)
+    B_np = cfg["B"]
+    dev = torch.device("cuda", local)
+    words = torch.from_numpy(words_np).to(dev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    plan = ops.Plan(words, K)
+    torch.cuda.synchronize()
+    plan_ms = (time.perf_counter() - t0) * 1e3
+    info = plan.info()
+    # rotation set: 8 independent B and C buffers (256 MiB > L2)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(1234 + rank)
+    Bs = [torch.from_numpy(B_np).to(dev)] + [torch.randn(K, N, device=dev, generator=gen) for _ in range(ROTATE - 1)]
+    Cs = [torch.empty(M, N, device=dev) for _ in range(ROTATE)]
+    wsb = plan.workspace_bytes(N)
+    wsp = torch.empty(max(wsb, 16), dtype=torch.uint8, device=dev)
+    kernels_per_step = 2 if info["mode"] == capi.PLAN_PROTO else 1
+
+    def step(i):
+        ops.spmm(words, K, Bs[i % ROTATE], plan=plan, out=Cs[i % ROTATE], workspace=wsp)
+
+    for i in range(max(args.warmup, 3)):
+        step(i)
+    torch.cuda.synchronize()
+    # capture one rotation (8 steps) in a graph
+    g = torch.cuda.CUDAGraph()
+    stream = torch.cuda.Stream(device=dev)
+    stream.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(stream):
+        with torch.cuda.graph(g, stream=stream):
+            for i in range(ROTATE):
+                step(i)
+    torch.cuda.synchronize()
+    reps = max(1, (args.steps + ROTATE - 1) // ROTATE)
+    steps = reps * ROTATE
+    for _ in range(max(1, args.warmup // ROTATE)):
+        g.replay()
+    torch.cuda.synchronize()
+
+    sampler = ClockSampler(local) if rank == 0 else None
+    if sampler:
+        sampler.start()
+    # per-step timing (one graph of 8 steps per event pair), then the total
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * reps)]
+    barrier(ws)
+    torch.cuda.synchronize()
+    cur = torch.cuda.current_stream()
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(cur)
+    for r in range(reps):
+        ev[2 * r].record(cur)
+        g.replay()
+        ev[2 * r + 1].record(cur)
+    t_end.record(cur)
+    torch.cuda.synchronize()
+    barrier(ws)
+    clocks = sampler.stop() if sampler else None
+    total_ms = t_start.elapsed_time(t_end)
+    rep_ms = [ev[2 * r].elapsed_time(ev[2 * r + 1]) for r in range(reps)]
+    total_ms = max_over_ranks(ws, total_ms)
+    ms_step = total_ms / steps
+    value = ws * comp_bytes / (ms_step * 1e-3) / 1e9
+    launch_ms = float(np.mean(rep_ms)) / ROTATE
+
+    # correctness spot check of the last rotation against a direct walk
+    Cd = ops.spmm(words, K, Bs[0])
+    torch.cuda.synchronize()
+    err = (Cs[0] - Cd).abs().max().item() / max(Cd.abs().max().item(), 1e-30)
+
+    # e2e through the public API: pinned host A words and B in, C out, plan built per step
+    h_words = torch.from_numpy(words_np).pin_memory()
+    h_B = torch.from_numpy(B_np).pin_memory()
+    h_C = torch.empty((M, N), dtype=torch.float32).pin_memory()
+    d_words = torch.empty_like(words)
+    d_B = torch.empty((K, N), device=dev)
+    d_C = torch.empty((M, N), device=dev)
+
+    def e2e_step(reuse_plan):
+        d_words.copy_(h_words, non_blocking=True)
+        d_B.copy_(h_B, non_blocking=True)
+        p = plan if reuse_plan else ops.Plan(d_words, K)
+        ops.spmm(d_words, K, d_B, plan=p, out=d_C, workspace=wsp if reuse_plan else None)
+        h_C.copy_(d_C, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        if not reuse_plan:
+            p.close()
+
+    e2e = {}
+    for reuse in (False, True):
+        for _ in range(2):
+            e2e_step(reuse)
+        barrier(ws)
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            e2e_step(reuse)
+        dt = max_over_ranks(ws, (time.perf_counter() - t0) / args.e2e_steps)
+        e2e[reuse] = ws * comp_bytes / dt / 1e9
+    e2e_matches = bool(np.array_equal(h_C.numpy(), Cs[0].cpu().numpy()))
+
+    peak, peak_kind = peaks()
+    achieved = comp_bytes / (launch_ms * 1e-3) / 1e9
+    traffic = traffic_from_profiles()
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded numpy clustered-rows A, N(0,1) B; 7 further random B in the rotation)",
+        "config": {"workload": "clustered_8192x8192x512_f32", "M": M, "K": K, "N": N,
+                   "l2": "inputs larger than L2: 8 rotating (B, C) pairs, 256 MiB",
+                   "plan_mode": "proto" if info["mode"] == capi.PLAN_PROTO else "direct",
+                   "plan_ms": plan_ms, "n_proto": info["n_proto"], "delta_nnz": info["delta_nnz"],
+                   "nnz": info["nnz"], "graph": "CUDA graph of 8 steps, replayed"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": peak_kind,
+                     "units": "compulsory bytes of one SpMM call (proto sums + row kernel)"},
+        "e2e": {"value": e2e[False], "unit": UNIT, "h2d_bytes_per_step": bA + bB,
+                "d2h_bytes_per_step": bC, "includes": "H2D A words + B, plan build, SpMM, D2H C",
+                "plan_reused_value": e2e[True]},
+        "gpu_launches": steps * kernels_per_step,
+        "clocks": clocks,
+        "max_rel_diff_vs_direct": err,
+        "e2e_output_matches_graph_output": e2e_matches,
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        t_full, sample = cpu_reference(cfg, cpu_sample_rows(cfg, args.cpu_seconds, threads), threads)
+        out["cpu_baseline"] = {"value": comp_bytes / t_full / 1e9, "unit": UNIT,
+                               "cores": os.cpu_count() or 1, "kind": "port", "sample": sample}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    plan.close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,76 @@
+// bsp_internal.cuh — helpers shared by the library's translation units.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "bsp.h"
+
+namespace bsp {
+
+// Records the cudaError_t of the most recent failure on this host thread.
+int cuda_status(cudaError_t e);
+
+#define BSP_TRY(x)                         \
+  do {                                     \
+    int bsp_s_ = (x);                      \
+    if (bsp_s_ != BSP_OK) return bsp_s_;   \
+  } while (0)
+
+#define BSP_CUDA(x)                                          \
+  do {                                                       \
+    cudaError_t bsp_e_ = (x);                                \
+    if (bsp_e_ != cudaSuccess) return ::bsp::cuda_status(bsp_e_); \
+  } while (0)
+
+#define BSP_LAUNCHED() BSP_CUDA(cudaPeekAtLastError())
+
+inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+inline bool is_aligned(const void* p, size_t a) { return (reinterpret_cast<uintptr_t>(p) % a) == 0; }
+inline int dtype_size(int dt) {
+  switch (dt) {
+    case BSP_F32: return 4;
+    case BSP_F16:
+    case BSP_BF16: return 2;
+    case BSP_I8:
+    case BSP_U8: return 1;
+    default: return 0;
+  }
+}
+
+// SM count of the current device (cached per device ordinal).
+int num_sms();
+
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ float to_f32(float x) { return x; }
+__device__ __forceinline__ float to_f32(__nv_bfloat16 x) { return __bfloat162float(x); }
+__device__ __forceinline__ float to_f32(__half x) { return __half2float(x); }
+
+// Internal launchers (defined in the .cu files, called from capi.cu).
+int launch_pack_rows(const void* dense, int dtype, int64_t M, int64_t K, int64_t ld,
+                     uint32_t* words, int msb, cudaStream_t s);
+int launch_pack_cols(const void* dense, int dtype, int64_t M, int64_t K, int64_t ld,
+                     uint32_t* words_t, int msb, cudaStream_t s);
+int launch_transpose_bits(const uint32_t* words, int64_t M, int64_t K, uint32_t* words_t,
+                          cudaStream_t s);
+int launch_unpack_rows(const uint32_t* words, int64_t M, int64_t K, void* dense, int dtype,
+                       int64_t ld, int msb, cudaStream_t s);
+int launch_bitplanes(const uint8_t* v, int64_t M, int64_t K, int64_t ld, int planes,
+                     uint32_t* words, int msb, cudaStream_t s);
+int launch_group_rows(const uint32_t* words, int64_t M, int64_t Kw, int tile_rows,
+                      int max_groups, int32_t* group_id, uint32_t* group_mask,
+                      int32_t* group_row, int32_t* spill_cnt, int32_t* spill_nnz,
+                      int32_t* spill_rows, int64_t* grouped_nnz, cudaStream_t s);
+int launch_group_to_dense(const float* gv, const int32_t* gid, const uint32_t* words,
+                          int64_t M, int64_t K, int tile_rows, int max_groups, float* dense,
+                          int64_t ldd, cudaStream_t s);
+
+// Exclusive prefix sum of n int32 values into out[0..n] (out[n] = total).
+// ws must hold scan_workspace_bytes(n) bytes.
+size_t scan_workspace_bytes(int64_t n);
+int launch_scan_i32(const int32_t* in, int64_t n, int32_t* out, void* ws, cudaStream_t s);
+
+}  // namespace bsp

@@ -1,0 +1,273 @@
+// capi.cu — the extern "C" entry points of include/bsp.h: argument
+// validation, layout checks and dispatch to the kernels.  Every entry point
+// returns a bsp_status and never aborts (the reference's CHECK_* macros
+// printed and returned EXIT_FAILURE, source/src/common.h:37-55).
+#include <climits>
+#include <new>
+
+#include "bsp_internal.cuh"
+#include "plan.cuh"
+#include "spmm.cuh"
+
+namespace bsp {
+
+static thread_local int g_last_cuda_error = 0;
+
+int cuda_status(cudaError_t e) {
+  if (e == cudaSuccess) return BSP_OK;
+  g_last_cuda_error = (int)e;
+  return BSP_ERR_CUDA;
+}
+
+int num_sms() {
+  static int cache[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 148;
+  if (cache[dev] == 0) {
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 148;
+    cache[dev] = n;
+  }
+  return cache[dev];
+}
+
+}  // namespace bsp
+
+using namespace bsp;
+
+namespace {
+
+constexpr int64_t kMaxCols = (int64_t)INT_MAX - 64;  // column indices are int32 on the device
+
+bool valid_dtype(int dt) { return dt >= BSP_F32 && dt <= BSP_U8; }
+bool valid_order(int o) { return o == BSP_LSB_FIRST || o == BSP_MSB_FIRST; }
+
+int check_dims(int64_t M, int64_t K) {
+  if (M < 0 || K < 0) return BSP_ERR_INVALID_ARG;
+  if (K > kMaxCols || M > kMaxCols) return BSP_ERR_CAPACITY;
+  return BSP_OK;
+}
+
+int current_device() {
+  int d = -1;
+  cudaGetDevice(&d);
+  return d;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* bsp_status_string(int status) {
+  switch (status) {
+    case BSP_OK: return "BSP_OK";
+    case BSP_ERR_INVALID_ARG: return "BSP_ERR_INVALID_ARG: invalid argument";
+    case BSP_ERR_ALIGNMENT: return "BSP_ERR_ALIGNMENT: misaligned pointer or leading dimension";
+    case BSP_ERR_WORKSPACE: return "BSP_ERR_WORKSPACE: workspace missing or too small";
+    case BSP_ERR_UNSUPPORTED: return "BSP_ERR_UNSUPPORTED: unsupported combination";
+    case BSP_ERR_CUDA: return "BSP_ERR_CUDA: CUDA runtime error";
+    case BSP_ERR_DEVICE_TIMEOUT: return "BSP_ERR_DEVICE_TIMEOUT: bounded device wait expired";
+    case BSP_ERR_ALLOC: return "BSP_ERR_ALLOC: allocation failed";
+    case BSP_ERR_CAPACITY: return "BSP_ERR_CAPACITY: size limit exceeded";
+    case BSP_ERR_QUEUE: return "BSP_ERR_QUEUE: corrupt work-queue descriptor";
+    case BSP_ERR_INTERNAL: return "BSP_ERR_INTERNAL: internal error";
+    default: return "unknown bsp status";
+  }
+}
+
+int bsp_version(void) { return 100; }
+
+int bsp_last_cuda_error(void) { return g_last_cuda_error; }
+
+int bsp_pack_rows(const void* dense, int dtype, int64_t M, int64_t K, int64_t ld, uint32_t* words,
+                  int bit_order, bsp_stream_t stream) {
+  BSP_TRY(check_dims(M, K));
+  if (!valid_dtype(dtype) || !valid_order(bit_order) || ld < K) return BSP_ERR_INVALID_ARG;
+  if (M == 0 || K == 0) return BSP_OK;
+  if (!dense || !words) return BSP_ERR_INVALID_ARG;
+  if (!is_aligned(dense, dtype_size(dtype)) || !is_aligned(words, 4)) return BSP_ERR_ALIGNMENT;
+  return launch_pack_rows(dense, dtype, M, K, ld, words, bit_order, (cudaStream_t)stream);
+}
+
+int bsp_pack_cols(const void* dense, int dtype, int64_t M, int64_t K, int64_t ld, uint32_t* words_t,
+                  int bit_order, bsp_stream_t stream) {
+  BSP_TRY(check_dims(M, K));
+  if (!valid_dtype(dtype) || !valid_order(bit_order) || ld < K) return BSP_ERR_INVALID_ARG;
+  if (M == 0 || K == 0) return BSP_OK;
+  if (!dense || !words_t) return BSP_ERR_INVALID_ARG;
+  if (!is_aligned(dense, dtype_size(dtype)) || !is_aligned(words_t, 4)) return BSP_ERR_ALIGNMENT;
+  return launch_pack_cols(dense, dtype, M, K, ld, words_t, bit_order, (cudaStream_t)stream);
+}
+
+int bsp_transpose_bits(const uint32_t* words, int64_t M, int64_t K, uint32_t* words_t,
+                       bsp_stream_t stream) {
+  BSP_TRY(check_dims(M, K));
+  if (M == 0 || K == 0) return BSP_OK;
+  if (!words || !words_t) return BSP_ERR_INVALID_ARG;
+  if (!is_aligned(words, 4) || !is_aligned(words_t, 4)) return BSP_ERR_ALIGNMENT;
+  return launch_transpose_bits(words, M, K, words_t, (cudaStream_t)stream);
+}
+
+int bsp_unpack_rows(const uint32_t* words, int64_t M, int64_t K, void* dense, int dtype, int64_t ld,
+                    int bit_order, bsp_stream_t stream) {
+  BSP_TRY(check_dims(M, K));
+  if (!valid_dtype(dtype) || !valid_order(bit_order) || ld < K) return BSP_ERR_INVALID_ARG;
+  if (M == 0 || K == 0) return BSP_OK;
+  if (!dense || !words) return BSP_ERR_INVALID_ARG;
+  if (!is_aligned(dense, dtype_size(dtype)) || !is_aligned(words, 4)) return BSP_ERR_ALIGNMENT;
+  return launch_unpack_rows(words, M, K, dense, dtype, ld, bit_order, (cudaStream_t)stream);
+}
+
+int bsp_bitplanes(const uint8_t* values, int64_t M, int64_t K, int64_t ld, int planes,
+                  uint32_t* words, int bit_order, bsp_stream_t stream) {
+  BSP_TRY(check_dims(M, K));
+  if (planes < 1 || planes > 8 || !valid_order(bit_order) || ld < K) return BSP_ERR_INVALID_ARG;
+  if (M == 0 || K == 0) return BSP_OK;
+  if (!values || !words) return BSP_ERR_INVALID_ARG;
+  if (!is_aligned(words, 4)) return BSP_ERR_ALIGNMENT;
+  return launch_bitplanes(values, M, K, ld, planes, words, bit_order, (cudaStream_t)stream);
+}
+
+int bsp_group_rows(const uint32_t* words, int64_t M, int64_t Kw, int tile_rows, int max_groups,
+                   int32_t* group_id, uint32_t* group_mask, int32_t* group_row, int32_t* spill_cnt,
+                   int32_t* spill_nnz, int32_t* spill_rows, int64_t* grouped_nnz,
+                   bsp_stream_t stream) {
+  if (M < 0 || Kw < 0) return BSP_ERR_INVALID_ARG;
+  if (tile_rows < 1 || tile_rows > 4096 || max_groups < 1 || max_groups > 32) return BSP_ERR_INVALID_ARG;
+  if (Kw > kMaxCols / 32 || M > kMaxCols) return BSP_ERR_CAPACITY;
+  if (M > 0 && Kw > 0 && (!words || !group_id || !group_mask)) return BSP_ERR_INVALID_ARG;
+  if (grouped_nnz && !is_aligned(grouped_nnz, 8)) return BSP_ERR_ALIGNMENT;
+  return launch_group_rows(words, M, Kw, tile_rows, max_groups, group_id, group_mask, group_row,
+                           spill_cnt, spill_nnz, spill_rows, grouped_nnz, (cudaStream_t)stream);
+}
+
+int bsp_group_to_dense(const float* group_values, const int32_t* group_id, const uint32_t* words,
+                       int64_t M, int64_t K, int tile_rows, int max_groups, float* dense,
+                       int64_t ldd, bsp_stream_t stream) {
+  BSP_TRY(check_dims(M, K));
+  if (tile_rows < 1 || tile_rows > 4096 || max_groups < 1 || max_groups > 32 || ldd < K)
+    return BSP_ERR_INVALID_ARG;
+  if (M == 0 || K == 0) return BSP_OK;
+  if (!group_values || !group_id || !words || !dense) return BSP_ERR_INVALID_ARG;
+  return launch_group_to_dense(group_values, group_id, words, M, K, tile_rows, max_groups, dense,
+                               ldd, (cudaStream_t)stream);
+}
+
+int bsp_plan_create(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_params* params,
+                    bsp_plan** plan, bsp_stream_t stream) {
+  if (!plan) return BSP_ERR_INVALID_ARG;
+  *plan = nullptr;
+  BSP_TRY(check_dims(M, K));
+  if (M > 0 && K > 0 && !words) return BSP_ERR_INVALID_ARG;
+  bsp_plan_params prm = {BSP_PLAN_AUTO, 4, 4, 0x5eed1234u};
+  if (params) {
+    if (params->mode < BSP_PLAN_AUTO || params->mode > BSP_PLAN_PROTO) return BSP_ERR_INVALID_ARG;
+    if (params->signature_hashes < 0 || params->signature_hashes > 8) return BSP_ERR_INVALID_ARG;
+    if (params->min_cluster_rows < 0) return BSP_ERR_INVALID_ARG;
+    prm.mode = params->mode;
+    if (params->signature_hashes) prm.signature_hashes = params->signature_hashes;
+    if (params->min_cluster_rows) prm.min_cluster_rows = params->min_cluster_rows;
+    prm.seed = params->seed ? params->seed : prm.seed;
+  }
+  if (prm.min_cluster_rows < 2) prm.min_cluster_rows = 2;
+  bsp_plan* p = new (std::nothrow) bsp_plan();
+  if (!p) return BSP_ERR_ALLOC;
+  p->device = current_device();
+  int st = BSP_OK;
+  if (M > 0 && K > 0) {
+    st = plan_build(words, M, K, &prm, p, (cudaStream_t)stream);
+  } else {
+    p->M = M;
+    p->K = K;
+    p->Kw = ceil_div(K, 32);
+  }
+  if (st != BSP_OK) {
+    plan_free(p);
+    delete p;
+    return st;
+  }
+  *plan = p;
+  return BSP_OK;
+}
+
+int bsp_plan_destroy(bsp_plan* plan) {
+  if (!plan) return BSP_OK;
+  plan_free(plan);
+  delete plan;
+  return BSP_OK;
+}
+
+int bsp_plan_get_info(const bsp_plan* plan, bsp_plan_info* info) {
+  if (!plan || !info) return BSP_ERR_INVALID_ARG;
+  info->M = plan->M;
+  info->K = plan->K;
+  info->nnz = plan->nnz;
+  info->mode = plan->mode;
+  info->n_proto = plan->mode == BSP_PLAN_PROTO ? plan->n_proto : 0;
+  info->proto_nnz = plan->mode == BSP_PLAN_PROTO ? plan->proto_nnz : 0;
+  info->delta_nnz = plan->mode == BSP_PLAN_PROTO ? plan->delta_nnz : 0;
+  info->direct_rows = plan->mode == BSP_PLAN_PROTO ? plan->direct_rows : plan->M;
+  info->direct_nnz = plan->mode == BSP_PLAN_PROTO ? plan->direct_nnz : plan->nnz;
+  return BSP_OK;
+}
+
+static int64_t proto_ldp(int64_t N) { return (N + 7) / 8 * 8; }
+
+int bsp_spmm_workspace(const bsp_plan* plan, int64_t N, size_t* bytes) {
+  if (!bytes || N < 0) return BSP_ERR_INVALID_ARG;
+  *bytes = 0;
+  if (plan && plan->mode == BSP_PLAN_PROTO)
+    *bytes = sizeof(float) * (size_t)plan->n_proto * (size_t)proto_ldp(N) + 256;
+  return BSP_OK;
+}
+
+int bsp_spmm(const uint32_t* A_words, int64_t M, int64_t K, const void* B, int b_dtype,
+             int64_t ldb, int64_t N, float* C, int64_t ldc, const bsp_plan* plan, void* workspace,
+             size_t workspace_bytes, bsp_stream_t stream) {
+  BSP_TRY(check_dims(M, K));
+  if (N < 0 || N > kMaxCols) return BSP_ERR_INVALID_ARG;
+  if (b_dtype != BSP_F32 && b_dtype != BSP_BF16 && b_dtype != BSP_F16) return BSP_ERR_UNSUPPORTED;
+  if (ldb < N || ldc < N) return BSP_ERR_INVALID_ARG;
+  if (plan && (plan->M != M || plan->K != K)) return BSP_ERR_INVALID_ARG;
+  if (plan && plan->device != current_device()) return BSP_ERR_INVALID_ARG;
+  if (M == 0 || N == 0) return BSP_OK;
+  if (!C || (K > 0 && (!A_words || !B))) return BSP_ERR_INVALID_ARG;
+  const int esz = dtype_size(b_dtype);
+  if (!is_aligned(B, esz) || !is_aligned(C, 4) || !is_aligned(A_words, 4)) return BSP_ERR_ALIGNMENT;
+  const cudaStream_t s = (cudaStream_t)stream;
+  if (K == 0) {  // C = 0
+    BSP_CUDA(cudaMemset2DAsync(C, sizeof(float) * ldc, 0, sizeof(float) * N, M, s));
+    return BSP_OK;
+  }
+  const int vcols = b_dtype == BSP_F32 ? 4 : 8;
+  const bool vec = is_aligned(B, 16) && ((ldb * esz) % 16 == 0) && (N % vcols == 0) &&
+                   is_aligned(C, 16) && (ldc % 4 == 0);
+  SpmmArgs a = {};
+  a.A = A_words;
+  a.M = M;
+  a.K = K;
+  a.Kw = ceil_div(K, 32);
+  a.B = B;
+  a.bdt = b_dtype;
+  a.ldb = ldb;
+  a.N = N;
+  a.C = C;
+  a.ldc = ldc;
+  const bool proto = plan && plan->mode == BSP_PLAN_PROTO && vec;
+  if (proto) {
+    size_t need = 0;
+    bsp_spmm_workspace(plan, N, &need);
+    if (!workspace || workspace_bytes < need) return BSP_ERR_WORKSPACE;
+    a.row_cluster = plan->row_cluster;
+    a.delta_ptr = plan->delta_ptr;
+    a.delta_idx = plan->delta_idx;
+    a.cons = plan->cons;
+    a.n_proto = plan->n_proto;
+    a.P = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255));
+    a.ldp = proto_ldp(N);
+    BSP_TRY(launch_proto_sums(a, s));
+  }
+  return launch_spmm_rows(a, proto, vec, s);
+}
+
+}  // extern "C"

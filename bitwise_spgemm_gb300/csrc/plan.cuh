@@ -1,0 +1,23 @@
+// plan.cuh — the plan object behind the opaque bsp_plan handle.
+#pragma once
+#include "bsp_internal.cuh"
+
+struct bsp_plan {
+  int64_t M = 0, K = 0, Kw = 0;
+  int mode = BSP_PLAN_DIRECT;
+  int device = 0;
+  int64_t nnz = 0, n_proto = 0, proto_nnz = 0, delta_nnz = 0, direct_rows = 0, direct_nnz = 0;
+  // device storage (owned)
+  void* arena = nullptr;        // row_cluster, delta_ptr, cons
+  void* delta_arena = nullptr;  // delta_idx
+  int32_t* row_cluster = nullptr;
+  int32_t* delta_ptr = nullptr;
+  uint32_t* delta_idx = nullptr;
+  uint32_t* cons = nullptr;
+};
+
+namespace bsp {
+int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_params* prm,
+               bsp_plan* plan, cudaStream_t s);
+void plan_free(bsp_plan* plan);
+}  // namespace bsp

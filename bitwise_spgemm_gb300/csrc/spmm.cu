@@ -1,0 +1,407 @@
+// spmm.cu — CUDA-core bitmap SpMM kernels: C[M×N] = A·B, A packed LSB-first.
+//
+// "Multiply by one replaced by adds": row i of C is the sum of the rows k of
+// B at A's set bits (reference backup/layout_trans.cu:158-171 did one global
+// atomicAdd per set bit and column).  Here one warp owns a row and a chunk of
+// columns, walks the row's set bits with __ffs in ascending column order,
+// gathers D rows of B at a time with 16-byte vector loads (D gathers in
+// flight per warp) and accumulates in FP32 registers in walk order.  Rows
+// with more than 4096 set bits use a compensated two-term (TwoSum)
+// accumulator.  Every output element is written once, without atomics, so
+// results are deterministic run to run.
+//
+// Prototype mode (plans from plan.cu): a row i in cluster c is
+//   C[i] = P[c] + Σ_{k ∈ A_i \ cons_c} B[k] − Σ_{k ∈ cons_c \ A_i} B[k],
+// where P[c] = Σ_{k ∈ cons_c} B[k] is computed once per cluster by
+// k_proto_sums (K split across the warps of a CTA, fixed-order reduction).
+#include "bsp_internal.cuh"
+#include "spmm.cuh"
+
+namespace bsp {
+namespace {
+
+constexpr int kCompThreshold = 4096;  // set bits above which rows use TwoSum
+
+// ---- vector loads of B ----------------------------------------------------
+template <typename BT> struct Vec;
+template <> struct Vec<float> {
+  static constexpr int COLS = 4;
+  using Raw = float4;
+  __device__ static Raw load(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+  __device__ static void cvt(const Raw& r, float* o) { o[0] = r.x; o[1] = r.y; o[2] = r.z; o[3] = r.w; }
+};
+template <> struct Vec<__nv_bfloat16> {
+  static constexpr int COLS = 8;
+  using Raw = uint4;
+  __device__ static Raw load(const __nv_bfloat16* p) { return __ldg(reinterpret_cast<const uint4*>(p)); }
+  __device__ static void cvt(const Raw& r, float* o) {
+    const uint32_t u[4] = {r.x, r.y, r.z, r.w};
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      o[2 * j] = __uint_as_float(u[j] << 16);
+      o[2 * j + 1] = __uint_as_float(u[j] & 0xffff0000u);
+    }
+  }
+};
+template <> struct Vec<__half> {
+  static constexpr int COLS = 8;
+  using Raw = uint4;
+  __device__ static Raw load(const __half* p) { return __ldg(reinterpret_cast<const uint4*>(p)); }
+  __device__ static void cvt(const Raw& r, float* o) {
+    const uint32_t u[4] = {r.x, r.y, r.z, r.w};
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      __half2 h = *reinterpret_cast<const __half2*>(&u[j]);
+      float2 f = __half22float2(h);
+      o[2 * j] = f.x;
+      o[2 * j + 1] = f.y;
+    }
+  }
+};
+
+// ---- index streams --------------------------------------------------------
+// next() returns a raw entry: column in bits 0..30, bit 31 = subtract (delta
+// lists only); kEnd when exhausted.  All state is warp-uniform.
+constexpr uint32_t kEnd = 0xffffffffu;
+
+// Set-bit walker over words [w_begin, w_end) of one packed row: `my` is this
+// lane's word of the current 32-word group, `pending` the lanes whose words
+// still hold bits, `cur` the word being consumed; columns come out ascending.
+struct BitWalker {
+  const uint32_t* words;
+  int w_end, g, curbase, lane;
+  uint32_t my, pending, cur;
+  __device__ void init(const uint32_t* w, int w_begin, int w_end_, int lane_) {
+    words = w;
+    w_end = w_end_;
+    g = w_begin - 32;
+    my = pending = cur = 0u;
+    curbase = 0;
+    lane = lane_;
+  }
+  __device__ __forceinline__ uint32_t next() {
+    while (cur == 0u) {
+      if (pending == 0u) {
+        g += 32;
+        if (g >= w_end) return kEnd;
+        my = (g + lane < w_end) ? __ldg(words + g + lane) : 0u;
+        pending = __ballot_sync(kFull, my != 0u);
+        continue;
+      }
+      const int src = __ffs(pending) - 1;
+      pending &= pending - 1;
+      cur = __shfl_sync(kFull, my, src);
+      curbase = (g + src) * 32;
+    }
+    const int b = __ffs(cur) - 1;
+    cur &= cur - 1;
+    return (uint32_t)(curbase + b);
+  }
+};
+
+// Entries of a delta list, 32 loaded at a time and broadcast by shuffle.
+struct ListWalker {
+  const uint32_t* list;
+  int pos, end, base, lane;
+  uint32_t mine;
+  __device__ void init(const uint32_t* l, int b, int e, int lane_) {
+    list = l;
+    pos = b;
+    end = e;
+    base = b - 32;
+    lane = lane_;
+    mine = 0u;
+  }
+  __device__ __forceinline__ uint32_t next() {
+    if (pos >= end) return kEnd;
+    if (pos >= base + 32) {
+      base = pos;
+      mine = (pos + lane < end) ? __ldg(list + pos + lane) : 0u;
+    }
+    const uint32_t e = __shfl_sync(kFull, mine, pos - base);
+    pos++;
+    return e;
+  }
+};
+
+template <int VPL, int COLS, bool COMP>
+struct Acc {
+  float s[VPL][COLS];
+  float c[COMP ? VPL : 1][COMP ? COLS : 1];
+  __device__ __forceinline__ void zero() {
+#pragma unroll
+    for (int v = 0; v < VPL; v++)
+#pragma unroll
+      for (int j = 0; j < COLS; j++) {
+        s[v][j] = 0.f;
+        if (COMP) c[COMP ? v : 0][COMP ? j : 0] = 0.f;
+      }
+  }
+  __device__ __forceinline__ void add(int v, int j, float x) {
+    if (COMP) {  // TwoSum: s + x = t + e exactly; e accumulates separately
+      const float t = s[v][j] + x;
+      const float bp = t - s[v][j];
+      const float e = (s[v][j] - (t - bp)) + (x - bp);
+      s[v][j] = t;
+      c[COMP ? v : 0][COMP ? j : 0] += e;
+    } else {
+      s[v][j] += x;
+    }
+  }
+  __device__ __forceinline__ float result(int v, int j) const {
+    return COMP ? s[v][j] + c[COMP ? v : 0][COMP ? j : 0] : s[v][j];
+  }
+};
+
+// Gathers D rows of B at a time (this lane's VPL vectors of each) and adds
+// them in stream order; entries with bit 31 set are subtracted.
+template <typename BT, int VPL, int D, bool COMP, typename Walker>
+__device__ __forceinline__ void accumulate_walk(Walker& wk, const BT* __restrict__ B, int64_t ldb,
+                                                const int* col, const bool* cvalid,
+                                                Acc<VPL, Vec<BT>::COLS, COMP>& acc) {
+  using V = Vec<BT>;
+  while (true) {
+    uint32_t idx[D];
+#pragma unroll
+    for (int s = 0; s < D; s++) idx[s] = wk.next();
+    if (idx[0] == kEnd) break;
+    typename V::Raw raw[D][VPL];
+#pragma unroll
+    for (int s = 0; s < D; s++) {
+      const BT* brow = B + (int64_t)(idx[s] & 0x7fffffffu) * ldb;
+#pragma unroll
+      for (int v = 0; v < VPL; v++)
+        if (idx[s] != kEnd && cvalid[v]) raw[s][v] = V::load(brow + col[v]);
+    }
+#pragma unroll
+    for (int s = 0; s < D; s++) {
+      if (idx[s] == kEnd) continue;
+      const bool neg = (idx[s] >> 31) != 0u;
+#pragma unroll
+      for (int v = 0; v < VPL; v++) {
+        if (!cvalid[v]) continue;
+        float f[V::COLS];
+        V::cvt(raw[s][v], f);
+#pragma unroll
+        for (int j = 0; j < V::COLS; j++) acc.add(v, j, neg ? -f[j] : f[j]);
+      }
+    }
+    if (idx[D - 1] == kEnd) break;
+  }
+}
+
+__device__ __forceinline__ int row_popcount(const uint32_t* __restrict__ row, int Kw, int lane) {
+  int c = 0;
+  for (int w = lane; w < Kw; w += 32) c += __popc(__ldg(row + w));
+#pragma unroll
+  for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(kFull, c, o);
+  return c;
+}
+
+template <int VPL, int COLS, bool COMP>
+__device__ __forceinline__ void store_vecs(float* __restrict__ crow, const int* col,
+                                           const bool* cvalid, const Acc<VPL, COLS, COMP>& acc,
+                                           const float* __restrict__ prow) {
+#pragma unroll
+  for (int v = 0; v < VPL; v++) {
+    if (!cvalid[v]) continue;
+    float o[COLS];
+#pragma unroll
+    for (int j = 0; j < COLS; j++) o[j] = acc.result(v, j);
+    if (prow) {
+#pragma unroll
+      for (int j = 0; j < COLS; j += 4) {
+        const float4 p = *reinterpret_cast<const float4*>(prow + col[v] + j);
+        o[j] += p.x; o[j + 1] += p.y; o[j + 2] += p.z; o[j + 3] += p.w;
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < COLS; j += 4)
+      *reinterpret_cast<float4*>(crow + col[v] + j) = make_float4(o[j], o[j + 1], o[j + 2], o[j + 3]);
+  }
+}
+
+// One warp per (row, column chunk of 32*VPL*COLS).  In PROTO launches, rows
+// with a cluster walk their delta list and add P[c]; every other row walks
+// A's words.  Rows with more than kCompThreshold set bits are summed with
+// TwoSum one column vector at a time, which keeps the wide path's register
+// budget unchanged.
+template <typename BT, int VPL, int D, bool PROTO>
+__global__ void __launch_bounds__(256) k_spmm_rows(SpmmArgs a) {
+  using V = Vec<BT>;
+  constexpr int COLS = V::COLS;
+  constexpr int CW = 32 * VPL * COLS;
+  const int lane = threadIdx.x & 31;
+  const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (row >= a.M) return;
+  const int n0 = (int)blockIdx.y * CW;
+  const BT* __restrict__ B = static_cast<const BT*>(a.B);
+  int col[VPL];
+  bool cvalid[VPL];
+#pragma unroll
+  for (int v = 0; v < VPL; v++) {
+    col[v] = n0 + (v * 32 + lane) * COLS;
+    cvalid[v] = col[v] < a.N;
+  }
+  float* crow = a.C + row * a.ldc;
+  if (PROTO) {
+    const int cl = __ldg(a.row_cluster + row);
+    if (cl >= 0) {
+      ListWalker wk;
+      wk.init(a.delta_idx, __ldg(a.delta_ptr + row), __ldg(a.delta_ptr + row + 1), lane);
+      Acc<VPL, COLS, false> acc;
+      acc.zero();
+      accumulate_walk<BT, VPL, D, false>(wk, B, a.ldb, col, cvalid, acc);
+      store_vecs<VPL, COLS, false>(crow, col, cvalid, acc, a.P + (int64_t)cl * a.ldp);
+      return;
+    }
+  }
+  const uint32_t* arow = a.A + row * a.Kw;
+  const int nnz = row_popcount(arow, (int)a.Kw, lane);
+  if (nnz <= kCompThreshold) {
+    BitWalker wk;
+    wk.init(arow, 0, (int)a.Kw, lane);
+    Acc<VPL, COLS, false> acc;
+    acc.zero();
+    accumulate_walk<BT, VPL, D, false>(wk, B, a.ldb, col, cvalid, acc);
+    store_vecs<VPL, COLS, false>(crow, col, cvalid, acc, nullptr);
+  } else {
+    for (int v = 0; v < VPL; v++) {
+      BitWalker wk;
+      wk.init(arow, 0, (int)a.Kw, lane);
+      Acc<1, COLS, true> acc;
+      acc.zero();
+      int c1[1] = {col[v]};
+      bool ok[1] = {cvalid[v]};
+      accumulate_walk<BT, 1, 4, true>(wk, B, a.ldb, c1, ok, acc);
+      store_vecs<1, COLS, true>(crow, c1, ok, acc, nullptr);
+    }
+  }
+}
+
+// Scalar fallback for unaligned or ragged layouts: lane = column.
+template <typename BT>
+__global__ void __launch_bounds__(256) k_spmm_rows_scalar(SpmmArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (row >= a.M) return;
+  const BT* __restrict__ B = static_cast<const BT*>(a.B);
+  const uint32_t* arow = a.A + row * a.Kw;
+  const int nnz = row_popcount(arow, (int)a.Kw, lane);
+  const bool comp = nnz > kCompThreshold;
+  for (int64_t n0 = (int64_t)blockIdx.y * 32; n0 < a.N; n0 += (int64_t)gridDim.y * 32) {
+    const int64_t j = n0 + lane;
+    float s = 0.f, c = 0.f;
+    BitWalker wk;
+    wk.init(arow, 0, (int)a.Kw, lane);
+    for (uint32_t k = wk.next(); k != kEnd; k = wk.next()) {
+      const float x = j < a.N ? to_f32(B[(int64_t)k * a.ldb + j]) : 0.f;
+      if (comp) {
+        const float t = s + x, bp = t - s;
+        c += (s - (t - bp)) + (x - bp);
+        s = t;
+      } else {
+        s += x;
+      }
+    }
+    if (j < a.N) a.C[row * a.ldc + j] = comp ? s + c : s;
+  }
+}
+
+// P[c][n0 .. n0+32*COLS) for one prototype per CTA row: warp w walks the
+// prototype's words [w*Kw/W, (w+1)*Kw/W), partial sums meet in shared memory
+// and are added in warp order.
+template <typename BT, int D>
+__global__ void __launch_bounds__(512) k_proto_sums(SpmmArgs a) {
+  using V = Vec<BT>;
+  constexpr int COLS = V::COLS;
+  constexpr int CW = 32 * COLS;
+  extern __shared__ float part[];  // [W][CW]
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, W = blockDim.x >> 5;
+  const int64_t c = blockIdx.x;
+  const int64_t n0 = (int64_t)blockIdx.y * CW;
+  const BT* __restrict__ B = static_cast<const BT*>(a.B);
+  int col[1] = {(int)n0 + lane * COLS};
+  bool cvalid[1] = {col[0] < a.N};
+  const uint32_t* cw = a.cons + c * a.Kw;
+  const int w0 = (int)(a.Kw * wid / W), w1 = (int)(a.Kw * (wid + 1) / W);
+  BitWalker wk;
+  wk.init(cw, w0, w1, lane);
+  Acc<1, COLS, false> acc;
+  acc.zero();
+  accumulate_walk<BT, 1, D, false>(wk, B, a.ldb, col, cvalid, acc);
+#pragma unroll
+  for (int j = 0; j < COLS; j++) part[wid * CW + lane * COLS + j] = acc.result(0, j);
+  __syncthreads();
+  for (int j = threadIdx.x; j < CW; j += blockDim.x) {
+    float s = 0.f;
+    for (int w = 0; w < W; w++) s += part[w * CW + j];
+    if (n0 + j < a.N) a.P[c * a.ldp + n0 + j] = s;
+  }
+}
+
+template <typename BT>
+int launch_rows_t(const SpmmArgs& a, bool proto, bool vec, cudaStream_t s) {
+  constexpr int COLS = Vec<BT>::COLS;
+  const unsigned gx = (unsigned)ceil_div(a.M, 8);
+  if (!vec) {
+    if (proto) return BSP_ERR_INTERNAL;
+    const int64_t gy = ceil_div(a.N, 32) < 65535 ? ceil_div(a.N, 32) : 65535;
+    k_spmm_rows_scalar<BT><<<dim3(gx, (unsigned)gy), 256, 0, s>>>(a);
+    BSP_LAUNCHED();
+    return BSP_OK;
+  }
+  // columns per warp: up to 4 vectors per lane for FP32, 2 for 16-bit B
+  constexpr int VPL_MAX = COLS == 4 ? 4 : 2;
+  const int64_t per1 = 32 * COLS;
+  if (a.N <= per1) {
+    const dim3 g(gx, (unsigned)ceil_div(a.N, per1));
+    if (proto) k_spmm_rows<BT, 1, 16, true><<<g, 256, 0, s>>>(a);
+    else k_spmm_rows<BT, 1, 16, false><<<g, 256, 0, s>>>(a);
+  } else if (a.N <= 2 * per1 || VPL_MAX == 2) {
+    const dim3 g(gx, (unsigned)ceil_div(a.N, 2 * per1));
+    if (proto) k_spmm_rows<BT, 2, 8, true><<<g, 256, 0, s>>>(a);
+    else k_spmm_rows<BT, 2, 8, false><<<g, 256, 0, s>>>(a);
+  } else {
+    const dim3 g(gx, (unsigned)ceil_div(a.N, 4 * per1));
+    if (proto) k_spmm_rows<BT, 4, 4, true><<<g, 256, 0, s>>>(a);
+    else k_spmm_rows<BT, 4, 4, false><<<g, 256, 0, s>>>(a);
+  }
+  BSP_LAUNCHED();
+  return BSP_OK;
+}
+
+template <typename BT>
+int launch_proto_t(const SpmmArgs& a, cudaStream_t s) {
+  constexpr int CW = 32 * Vec<BT>::COLS;
+  const int threads = 512;
+  const size_t smem = (size_t)(threads / 32) * CW * sizeof(float);
+  const dim3 g((unsigned)a.n_proto, (unsigned)ceil_div(a.N, CW));
+  k_proto_sums<BT, 8><<<g, threads, smem, s>>>(a);
+  BSP_LAUNCHED();
+  return BSP_OK;
+}
+
+}  // namespace
+
+int launch_spmm_rows(const SpmmArgs& a, bool proto, bool vec, cudaStream_t s) {
+  if (a.M == 0 || a.N == 0) return BSP_OK;
+  switch (a.bdt) {
+    case BSP_F32: return launch_rows_t<float>(a, proto, vec, s);
+    case BSP_BF16: return launch_rows_t<__nv_bfloat16>(a, proto, vec, s);
+    case BSP_F16: return launch_rows_t<__half>(a, proto, vec, s);
+    default: return BSP_ERR_UNSUPPORTED;
+  }
+}
+
+int launch_proto_sums(const SpmmArgs& a, cudaStream_t s) {
+  if (a.n_proto == 0 || a.N == 0) return BSP_OK;
+  switch (a.bdt) {
+    case BSP_F32: return launch_proto_t<float>(a, s);
+    case BSP_BF16: return launch_proto_t<__nv_bfloat16>(a, s);
+    case BSP_F16: return launch_proto_t<__half>(a, s);
+    default: return BSP_ERR_UNSUPPORTED;
+  }
+}
+
+}  // namespace bsp

@@ -1,0 +1,29 @@
+// spmm.cuh — argument block and launchers of the CUDA-core SpMM kernels.
+#pragma once
+#include "bsp_internal.cuh"
+
+namespace bsp {
+
+struct SpmmArgs {
+  const uint32_t* A;  // packed rows [M][Kw], LSB-first
+  int64_t M, K, Kw;
+  const void* B;      // [K][ldb] of bdt
+  int bdt;
+  int64_t ldb, N;
+  float* C;           // [M][ldc]
+  int64_t ldc;
+  // prototype mode (plan)
+  const int32_t* row_cluster;  // [M], -1 = walk A's row
+  const int32_t* delta_ptr;    // [M+1]
+  const uint32_t* delta_idx;   // column | 0x80000000 for "subtract"
+  const uint32_t* cons;        // [n_proto][Kw] prototype masks
+  int64_t n_proto;
+  float* P;                    // [n_proto][ldp] prototype sums (workspace)
+  int64_t ldp;
+};
+
+// vec = B/C layouts allow 16-byte vector access (else lane-per-column path)
+int launch_spmm_rows(const SpmmArgs& a, bool proto, bool vec, cudaStream_t s);
+int launch_proto_sums(const SpmmArgs& a, cudaStream_t s);
+
+}  // namespace bsp

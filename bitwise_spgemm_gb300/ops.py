@@ -1,0 +1,174 @@
+"""Torch-tensor front end of the C ABI (device memory and streams from torch).
+
+Names follow include/bsp.h; each docstring names the reference kernel the
+call replaces.  Tensors must live on the current CUDA device; results are
+produced on torch's current stream.
+"""
+import ctypes as C
+
+import torch
+
+from . import capi
+from .capi import call
+
+_DT = {torch.float32: capi.F32, torch.float16: capi.F16, torch.bfloat16: capi.BF16,
+       torch.int8: capi.I8, torch.uint8: capi.U8}
+
+
+def _stream():
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _p(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _rowmajor(t, name):
+    if t.dim() != 2 or t.stride(1) != 1:
+        raise ValueError("%s must be a 2-D tensor with unit column stride" % name)
+    return t.stride(0)
+
+
+def words_per_row(k):
+    return (k + 31) // 32
+
+
+def pack_rows(dense, bit_order=capi.LSB_FIRST, out=None):
+    """dense [M, K] -> packed row masks int32 [M, ceil(K/32)] (uint32 bits).
+    Replaces dense2bitmask (reference source/src/main.cu:591-628)."""
+    ld = _rowmajor(dense, "dense")
+    M, K = dense.shape
+    if out is None:
+        out = torch.empty((M, words_per_row(K)), dtype=torch.int32, device=dense.device)
+    call("bsp_pack_rows", _p(dense), _DT[dense.dtype], M, K, ld, _p(out), bit_order, _stream())
+    return out
+
+
+def pack_cols(dense, bit_order=capi.LSB_FIRST, out=None):
+    """dense [M, K] -> column masks [K, ceil(M/32)] (packed rows of the transpose)."""
+    ld = _rowmajor(dense, "dense")
+    M, K = dense.shape
+    if out is None:
+        out = torch.empty((K, words_per_row(M)), dtype=torch.int32, device=dense.device)
+    call("bsp_pack_cols", _p(dense), _DT[dense.dtype], M, K, ld, _p(out), bit_order, _stream())
+    return out
+
+
+def transpose_bits(words, M, K, out=None):
+    if out is None:
+        out = torch.empty((K, words_per_row(M)), dtype=torch.int32, device=words.device)
+    call("bsp_transpose_bits", _p(words), M, K, _p(out), _stream())
+    return out
+
+
+def unpack_rows(words, M, K, dtype=torch.float32, bit_order=capi.LSB_FIRST, out=None):
+    """Packed masks -> dense 0/1 [M, K] (the scatter of group2dense for a full mask)."""
+    if out is None:
+        out = torch.empty((M, K), dtype=dtype, device=words.device)
+    ld = _rowmajor(out, "out")
+    call("bsp_unpack_rows", _p(words), M, K, _p(out), _DT[out.dtype], ld, bit_order, _stream())
+    return out
+
+
+def bitplanes(values, planes=8, bit_order=capi.LSB_FIRST, out=None):
+    """uint8/int8 [M, K] -> packed bit planes [planes, M, ceil(K/32)].
+    Replaces uint8_layout_trans (reference backup/layout_trans.cu:87-97)."""
+    ld = _rowmajor(values, "values")
+    M, K = values.shape
+    if out is None:
+        out = torch.empty((planes, M, words_per_row(K)), dtype=torch.int32, device=values.device)
+    call("bsp_bitplanes", _p(values), M, K, ld, planes, _p(out), bit_order, _stream())
+    return out
+
+
+def group_rows(words, tile_rows, max_groups):
+    """First-fit grouping of packed rows per (tile_rows × 32-column) tile.
+    Replaces generate_groups_large (reference source/src/main.cu:50-247)."""
+    M, Kw = words.shape
+    T = ((M + tile_rows - 1) // tile_rows) * Kw
+    dev = words.device
+    out = dict(
+        group_id=torch.empty((M, Kw), dtype=torch.int32, device=dev),
+        group_mask=torch.empty((T, max_groups), dtype=torch.int32, device=dev),
+        group_row=torch.empty((T, max_groups, 32), dtype=torch.int32, device=dev),
+        spill_cnt=torch.empty(T, dtype=torch.int32, device=dev),
+        spill_nnz=torch.empty(T, dtype=torch.int32, device=dev),
+        spill_rows=torch.empty((T, tile_rows), dtype=torch.int32, device=dev),
+        grouped_nnz=torch.empty(1, dtype=torch.int64, device=dev),
+    )
+    call("bsp_group_rows", _p(words), M, Kw, tile_rows, max_groups, _p(out["group_id"]),
+         _p(out["group_mask"]), _p(out["group_row"]), _p(out["spill_cnt"]), _p(out["spill_nnz"]),
+         _p(out["spill_rows"]), _p(out["grouped_nnz"]), _stream())
+    return out
+
+
+def group_to_dense(group_values, group_id, words, M, K, tile_rows, max_groups, out=None):
+    """Replaces group2dense (reference source/src/main.cu:829-850)."""
+    if out is None:
+        out = torch.zeros((M, K), dtype=torch.float32, device=words.device)
+    call("bsp_group_to_dense", _p(group_values), _p(group_id), _p(words), M, K, tile_rows,
+         max_groups, _p(out), out.stride(0), _stream())
+    return out
+
+
+class Plan:
+    """SpMM schedule for one A (similarity row grouping).  Owns device memory."""
+
+    def __init__(self, words, K, mode=capi.PLAN_AUTO, signature_hashes=0, min_cluster_rows=0,
+                 seed=0):
+        self.M, Kw = words.shape
+        self.K = K
+        if Kw != words_per_row(K):
+            raise ValueError("words has %d columns, expected ceil(K/32)=%d" % (Kw, words_per_row(K)))
+        prm = capi.PlanParams(mode, signature_hashes, min_cluster_rows, seed)
+        h = C.c_void_p()
+        call("bsp_plan_create", _p(words), self.M, K, C.byref(prm), C.byref(h), _stream())
+        self._h = h
+        self._lib = capi.lib()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def info(self):
+        inf = capi.PlanInfo()
+        call("bsp_plan_get_info", self._h, C.byref(inf))
+        return {f: getattr(inf, f) for f, _ in inf._fields_}
+
+    def workspace_bytes(self, N):
+        n = C.c_size_t()
+        call("bsp_spmm_workspace", self._h, N, C.byref(n))
+        return n.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.bsp_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+def spmm(words, K, B, plan=None, out=None, workspace=None):
+    """C = A·B, FP32 output.  A: packed rows [M, ceil(K/32)], B: [K, N]
+    float32/bfloat16/float16.  Replaces uint8_spmm_2d_1d / indexed_spmm
+    (reference backup/layout_trans.cu:120-171)."""
+    M = words.shape[0]
+    ldb = _rowmajor(B, "B")
+    if B.shape[0] != K:
+        raise ValueError("B must have K rows")
+    N = B.shape[1]
+    if out is None:
+        out = torch.empty((M, N), dtype=torch.float32, device=B.device)
+    ldc = _rowmajor(out, "out")
+    h = plan.handle if plan is not None else None
+    ws_ptr, ws_n = None, 0
+    if plan is not None:
+        need = plan.workspace_bytes(N)
+        if need:
+            if workspace is None or workspace.numel() * workspace.element_size() < need:
+                workspace = torch.empty(need, dtype=torch.uint8, device=B.device)
+            ws_ptr, ws_n = _p(workspace), workspace.numel() * workspace.element_size()
+    call("bsp_spmm", _p(words), M, K, _p(B), _DT[B.dtype], ldb, N, _p(out), ldc, h, ws_ptr, ws_n,
+         _stream())
+    return out

@@ -1,0 +1,198 @@
+"""SpMM on the GPU against the oracle (FP32 order-exact and FP64) and the
+reference fixtures.
+
+Tolerances: integer-valued B must match bit for bit.  Otherwise the error
+of every element is measured against the FP64 oracle relative to the scale
+of its summation bound, |C - C64| / (|A||B|)_ij, and must be ≤ 1e-5 for FP32
+B (the relative tolerance of the reference's check(),
+backup/bit_wise_gemm.cu:24); BF16/FP16 B is exact in FP32 so the same bound
+holds against the FP64 product of the rounded B.
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle as O
+from bitwise_spgemm_gb300 import capi, ops
+from bitwise_spgemm_gb300 import workloads as W
+from gpu_util import bf16_dev, words_dev
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+
+
+def _check_f64(C, words, K, Bf32, tol=TOL):
+    C64 = O.spmm_f64(words, K, Bf32)
+    Cabs = O.spmm_abs_f64(words, K, Bf32)
+    mx, mean, mxn = O.rel_errors(C, C64, Cabs)
+    assert mx <= tol, (mx, mean, mxn)
+    return mx, mean, mxn
+
+
+def test_reference_fixture_bit_exact(golden):
+    A = golden["spmm_A01"].astype(bool)
+    words = W.pack_bits(A)
+    wd = words_dev(words)
+    for bkey, ckey in (("spmm_B_int", "spmm_C_int_ref"), ("spmm_B_normal", "spmm_C_normal_ref")):
+        C = ops.spmm(wd, A.shape[1], torch.from_numpy(golden[bkey]).cuda()).cpu().numpy()
+        # ascending-column FP32 sums: the reference's own order, bit for bit
+        assert np.array_equal(C, golden[ckey]), bkey
+
+
+def test_config1_bit_exact():
+    cfg = W.config1()
+    wd = words_dev(cfg["words"])
+    B = torch.from_numpy(cfg["B"]).cuda()
+    C = ops.spmm(wd, cfg["K"], B).cpu().numpy()
+    ref = O.spmm_f32(cfg["words"], cfg["K"], cfg["B"])
+    assert np.array_equal(C, ref)
+    assert np.array_equal(C.astype(np.float64), O.spmm_f64(cfg["words"], cfg["K"], cfg["B"]))
+    # the plan path gives the same integers
+    plan = ops.Plan(wd, cfg["K"], mode=capi.PLAN_PROTO)
+    C2 = ops.spmm(wd, cfg["K"], B, plan=plan).cpu().numpy()
+    assert np.array_equal(C2, ref)
+
+
+@pytest.fixture(scope="module")
+def cfg2():
+    return W.config2()
+
+
+def test_config2_plan_and_tolerance(cfg2):
+    words, K, Bn = cfg2["words"], cfg2["K"], cfg2["B"]
+    wd = words_dev(words)
+    B = torch.from_numpy(Bn).cuda()
+    plan = ops.Plan(wd, K)
+    info = plan.info()
+    assert info["mode"] == capi.PLAN_PROTO
+    assert info["n_proto"] >= 64 and info["n_proto"] <= 80
+    # the delta lists are a small fraction of the set bits
+    assert info["delta_nnz"] + info["proto_nnz"] < 0.1 * info["nnz"]
+    C = ops.spmm(wd, K, B, plan=plan)
+    Cd = ops.spmm(wd, K, B)
+    _check_f64(C.cpu().numpy(), words, K, Bn)
+    _check_f64(Cd.cpu().numpy(), words, K, Bn)
+    # deterministic
+    assert torch.equal(C, ops.spmm(wd, K, B, plan=plan))
+    # integer B through the plan: bit-exact even with subtractions
+    Bi = np.random.default_rng(12).integers(-8, 9, (K, 512)).astype(np.float32)
+    Ci = ops.spmm(wd, K, torch.from_numpy(Bi).cuda(), plan=plan).cpu().numpy()
+    assert np.array_equal(Ci.astype(np.float64), O.spmm_f64(words, K, Bi))
+
+
+@pytest.mark.parametrize("M,K,N,p", [(1, 1, 1, 1.0), (37, 45, 7, 0.3), (64, 1000, 130, 0.1),
+                                     (300, 97, 512, 0.05), (128, 64, 1024, 0.5),
+                                     (17, 4096, 2048, 0.02)])
+@pytest.mark.parametrize("bdt", ["f32", "bf16", "f16"])
+def test_random_shapes(M, K, N, p, bdt):
+    rng = np.random.default_rng(M * 31 + K + N)
+    bits = rng.random((M, K)) < p
+    bits[0] = False  # empty row
+    words = W.pack_bits(bits)
+    Bf = rng.standard_normal((K, N)).astype(np.float32)
+    if bdt == "f32":
+        B = torch.from_numpy(Bf).cuda()
+    elif bdt == "bf16":
+        b16 = W.f32_to_bf16_bits(Bf)
+        Bf = W.bf16_bits_to_f32(b16)
+        B = bf16_dev(b16)
+    else:
+        B = torch.from_numpy(Bf).half().cuda()
+        Bf = B.float().cpu().numpy()
+    C = ops.spmm(words_dev(words), K, B).cpu().numpy()
+    assert np.all(C[0] == 0)
+    _check_f64(C, words, K, Bf)
+    if bdt == "f32":
+        assert np.array_equal(C, O.spmm_f32(words, K, Bf))
+
+
+def test_strided_operands():
+    rng = np.random.default_rng(5)
+    M, K, N = 100, 300, 96
+    bits = rng.random((M, K)) < 0.1
+    words = W.pack_bits(bits)
+    Bbig = torch.from_numpy(rng.standard_normal((K, N + 40)).astype(np.float32)).cuda()
+    B = Bbig[:, 8:8 + N]  # ldb = N + 40, 32-byte offset
+    Cbig = torch.full((M, N + 4), 7.0, device="cuda")
+    C = Cbig[:, :N]
+    ops.spmm(words_dev(words), K, B, out=C)
+    ref = O.spmm_f32(words, K, B.contiguous().cpu().numpy())
+    assert np.array_equal(C.cpu().numpy(), ref)
+    assert torch.all(Cbig[:, N:] == 7.0)
+    # unaligned B pointer (offset 1 element) takes the lane-per-column path
+    B1 = Bbig[:, 1:1 + N]
+    C1 = ops.spmm(words_dev(words), K, B1).cpu().numpy()
+    assert np.array_equal(C1, O.spmm_f32(words, K, B1.contiguous().cpu().numpy()))
+
+
+def test_heavy_rows_compensated():
+    rng = np.random.default_rng(7)
+    M, K, N = 8, 20000, 64
+    bits = rng.random((M, K)) < 0.6  # ~12000 set bits per row (> 4096)
+    words = W.pack_bits(bits)
+    Bf = (rng.standard_normal((K, N)) * 1e3 + 1.0).astype(np.float32)
+    C = ops.spmm(words_dev(words), K, torch.from_numpy(Bf).cuda()).cpu().numpy()
+    mx, _, _ = _check_f64(C, words, K, Bf)
+    # compensated sums are much closer to FP64 than the plain FP32 walk
+    C32 = O.spmm_f32(words, K, Bf)
+    C64 = O.spmm_f64(words, K, Bf)
+    assert np.abs(C - C64).max() < 0.5 * np.abs(C32 - C64).max()
+
+
+def test_empty_and_degenerate():
+    wd = torch.zeros((0, 2), dtype=torch.int32, device="cuda")
+    B = torch.randn(40, 8, device="cuda")
+    assert ops.spmm(wd, 40, B).shape == (0, 8)
+    wd = torch.zeros((5, 0), dtype=torch.int32, device="cuda")
+    C = ops.spmm(wd, 0, torch.zeros((0, 8), device="cuda"))
+    assert torch.all(C == 0)
+    # all-zero A, plan with no clusters
+    wd = torch.zeros((64, 4), dtype=torch.int32, device="cuda")
+    plan = ops.Plan(wd, 128)
+    assert plan.info()["mode"] == capi.PLAN_DIRECT
+    C = ops.spmm(wd, 128, torch.randn(128, 16, device="cuda"), plan=plan)
+    assert torch.all(C == 0)
+
+
+def test_plan_errors():
+    wd = torch.zeros((64, 4), dtype=torch.int32, device="cuda")
+    plan = ops.Plan(wd, 128)
+    with pytest.raises(capi.BspError):
+        ops.spmm(wd[:32], 128, torch.randn(128, 16, device="cuda"), plan=plan)
+    # proto plan with too-small workspace is rejected
+    rng = np.random.default_rng(3)
+    A, _, _ = W.clustered_bits(512, 1024, n_proto=4, p_proto=0.2)
+    words = W.pack_bits(A)
+    wdp = words_dev(words)
+    plan = ops.Plan(wdp, 1024, mode=capi.PLAN_PROTO)
+    assert plan.info()["mode"] == capi.PLAN_PROTO
+    need = plan.workspace_bytes(64)
+    ws = torch.empty(need - 300, dtype=torch.uint8, device="cuda")
+    import ctypes as C
+    Bt = torch.randn(1024, 64, device="cuda")
+    Ct = torch.empty(512, 64, device="cuda")
+    st = capi.lib().bsp_spmm(C.c_void_p(wdp.data_ptr()), 512, 1024, C.c_void_p(Bt.data_ptr()), 0, 64,
+                             64, C.c_void_p(Ct.data_ptr()), 64, plan.handle, C.c_void_p(ws.data_ptr()),
+                             ws.numel(), None)
+    assert st == -3
+    _ = rng
+
+
+def test_clustered_small_plans_all_modes():
+    A, _, _ = W.clustered_bits(2048, 2048, n_proto=16, p_proto=0.1, p_flip=0.01, seed_proto=21,
+                               seed_rows=22)
+    words = W.pack_bits(A)
+    wd = words_dev(words)
+    Bf = np.random.default_rng(23).standard_normal((2048, 256)).astype(np.float32)
+    B = torch.from_numpy(Bf).cuda()
+    outs = []
+    for mode in (capi.PLAN_AUTO, capi.PLAN_DIRECT, capi.PLAN_PROTO):
+        plan = ops.Plan(wd, 2048, mode=mode)
+        C = ops.spmm(wd, 2048, B, plan=plan).cpu().numpy()
+        _check_f64(C, words, 2048, Bf)
+        outs.append(C)
+    b16 = W.f32_to_bf16_bits(Bf)
+    plan = ops.Plan(wd, 2048, mode=capi.PLAN_PROTO)
+    C = ops.spmm(wd, 2048, bf16_dev(b16), plan=plan).cpu().numpy()
+    _check_f64(C, words, 2048, W.bf16_bits_to_f32(b16))
