@@ -332,7 +332,8 @@ def run_ours(args):
                    "l2": "inputs larger than L2: 8 rotating (B, C) pairs, 256 MiB",
                    "plan_mode": "proto" if info["mode"] == capi.PLAN_PROTO else "direct",
                    "plan_ms": plan_ms, "n_proto": info["n_proto"], "delta_nnz": info["delta_nnz"],
-                   "nnz": info["nnz"], "graph": "CUDA graph of 8 steps, replayed"},
+                   "nnz": info["nnz"], "direct_rows": info["direct_rows"],
+                   "graph": "CUDA graph of 8 steps, replayed"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_source": peak_kind,

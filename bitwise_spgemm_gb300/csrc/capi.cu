@@ -159,7 +159,7 @@ int bsp_plan_create(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_
   *plan = nullptr;
   BSP_TRY(check_dims(M, K));
   if (M > 0 && K > 0 && !words) return BSP_ERR_INVALID_ARG;
-  bsp_plan_params prm = {BSP_PLAN_AUTO, 4, 4, 0x5eed1234u};
+  bsp_plan_params prm = {BSP_PLAN_AUTO, 8, 4, 0x5eed1234u};
   if (params) {
     if (params->mode < BSP_PLAN_AUTO || params->mode > BSP_PLAN_PROTO) return BSP_ERR_INVALID_ARG;
     if (params->signature_hashes < 0 || params->signature_hashes > 8) return BSP_ERR_INVALID_ARG;

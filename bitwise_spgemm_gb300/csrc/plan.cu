@@ -10,15 +10,20 @@
 //  1. signatures: H MinHash values per row — h_j(row) = min over the row's
 //     set columns k of mix(k, j) — plus the row's popcount (warp per row,
 //     __popc + warp min-reduction);
-//  2. bucketing: rows with equal h_0 meet in an open-addressing hash table
-//     (atomicCAS insert, atomicAdd size, atomicMin leader = lowest row);
+//  2. bucketing: rows with equal band key (h_0, h_1, h_2) meet in an
+//     open-addressing hash table (atomicCAS insert, atomicAdd size,
+//     atomicMin leader = lowest row).  Two unrelated rows share one MinHash
+//     value with probability equal to their Jaccard similarity (≈2.5 % for
+//     two random 5 %-dense masks), so a single-hash key would merge clusters;
+//     the three-value band makes that ≈J³;
 //  3. buckets with ≥ min_cluster_rows rows become clusters, numbered by an
 //     exclusive scan over "row is a bucket leader" flags (stable: ascending
 //     leader row), so numbering is deterministic;
 //  4. consensus: per-cluster per-column counts (atomicAdd), majority bit;
-//  5. rows left out by step 3 look up the clusters whose consensus shares
-//     one of their other MinHash values h_1..h_{H-1} and take the nearest one
-//     (Hamming distance, ties → lower cluster id);
+//  5. every row also looks up, for each pair band (h_2b, h_2b+1), the
+//     cluster whose consensus has the same pair, and keeps the nearest
+//     candidate (Hamming distance, ties → lower cluster id) — this rescues
+//     rows whose band key in step 2 was disturbed by their own flips;
 //  6. every row keeps its cluster only if |row XOR consensus| < popcount(row);
 //     delta lists (ascending column, bit 31 = column present in the consensus
 //     but not in the row → subtract) are laid out by an exclusive scan.
@@ -46,6 +51,18 @@ __device__ __forceinline__ uint32_t mix32(uint32_t k, uint32_t j, uint32_t seed)
   h *= 0xc2b2ae35u;
   h ^= h >> 16;
   return h;
+}
+
+constexpr int kBand = 3;  // MinHash values in the bucket key
+
+__device__ __forceinline__ uint32_t band_key(const uint32_t* __restrict__ sig, int H) {
+  uint32_t k = 0x811c9dc5u;
+  for (int j = 0; j < kBand && j < H; j++) {
+    if (sig[j] == kEmpty) return kEmpty;
+    k = (k ^ sig[j]) * 0x01000193u;
+    k ^= k >> 15;
+  }
+  return k == kEmpty ? kEmpty - 1 : k;
 }
 
 __device__ __forceinline__ uint32_t slot_of(uint32_t key, uint32_t mask) {
@@ -87,13 +104,13 @@ __global__ void __launch_bounds__(256) k_signatures(const uint32_t* __restrict__
   if (lane == 0) nnz[row] = cnt;
 }
 
-// Thread per row: insert h_0 into the bucket table.
+// Thread per row: insert the row's band key into the bucket table.
 __global__ void k_bucket_insert(const uint32_t* __restrict__ sig, const int32_t* __restrict__ nnz,
                                 int64_t M, int H, uint32_t* keys, int32_t* count, int32_t* leader,
                                 uint32_t tmask, int32_t* __restrict__ row_slot) {
   const int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (row >= M) return;
-  const uint32_t key = sig[row * H];
+  const uint32_t key = band_key(sig + row * H, H);
   int32_t found = -1;
   if (nnz[row] > 0 && key != kEmpty) {
     uint32_t s = slot_of(key, tmask);
@@ -168,17 +185,27 @@ __global__ void k_majority(const int32_t* __restrict__ counts, const int32_t* __
   cons[t] = m;
 }
 
-// Tables j = 1..H-1: h_j(consensus c) → lowest c.
+__device__ __forceinline__ uint32_t pair_key(uint32_t a, uint32_t b) {
+  if (a == kEmpty || b == kEmpty) return kEmpty;
+  uint32_t k = (a * 0x9e3779b1u) ^ (b + 0x7f4a7c15u + (a << 6) + (a >> 2));
+  k ^= k >> 16;
+  k *= 0x85ebca6bu;
+  k ^= k >> 13;
+  return k == kEmpty ? kEmpty - 1 : k;
+}
+
+// Tables j = 0..H/2-1: pair band (h_2j, h_2j+1) of consensus c → lowest c.
 __global__ void k_alt_insert(const uint32_t* __restrict__ csig, int64_t n_clusters, int H,
                              uint32_t* keys, int32_t* vals, uint32_t tmask) {
+  const int NB = H / 2;
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= n_clusters * (H - 1)) return;
-  const int64_t c = t / (H - 1);
-  const int j = 1 + (int)(t - c * (H - 1));
-  const uint32_t key = csig[c * H + j];
+  if (t >= n_clusters * NB) return;
+  const int64_t c = t / NB;
+  const int j = (int)(t - c * NB);
+  const uint32_t key = pair_key(csig[c * H + 2 * j], csig[c * H + 2 * j + 1]);
   if (key == kEmpty) return;
-  uint32_t* K = keys + (int64_t)(j - 1) * (tmask + 1);
-  int32_t* V = vals + (int64_t)(j - 1) * (tmask + 1);
+  uint32_t* K = keys + (int64_t)j * (tmask + 1);
+  int32_t* V = vals + (int64_t)j * (tmask + 1);
   uint32_t s = slot_of(key, tmask);
   for (uint32_t probe = 0; probe <= tmask; probe++) {
     const uint32_t prev = atomicCAS(K + s, kEmpty, key);
@@ -209,8 +236,9 @@ __device__ __forceinline__ int xor_popcount(const uint32_t* __restrict__ a, cons
   return (int)__reduce_add_sync(kFull, (unsigned)d);
 }
 
-// Warp per row: leftover rows try their other MinHash buckets; every row
-// keeps its cluster only if the delta is smaller than its popcount.
+// Warp per row: the row's bucket cluster and the clusters sharing one of its
+// pair bands compete on Hamming distance; the row keeps the winner only if
+// the delta is smaller than its popcount.
 __global__ void __launch_bounds__(256) k_finalize_rows(
     const uint32_t* __restrict__ words, int64_t M, int Kw, int H, const uint32_t* __restrict__ sig,
     const int32_t* __restrict__ nnz, const uint32_t* __restrict__ cons, int64_t n_clusters,
@@ -224,21 +252,20 @@ __global__ void __launch_bounds__(256) k_finalize_rows(
   const int n = nnz[row];
   int c = cluster[row];
   int d = INT_MAX;
-  if (n > 0 && c < 0 && n_clusters > 0) {
-    for (int j = 1; j < H; j++) {
-      const uint32_t key = sig[row * H + j];
+  if (c >= 0) d = xor_popcount(r, cons + (int64_t)c * Kw, Kw, lane);
+  if (n > 0 && n_clusters > 0) {
+    for (int j = 0; j < H / 2; j++) {
+      const uint32_t key = pair_key(sig[row * H + 2 * j], sig[row * H + 2 * j + 1]);
       if (key == kEmpty) continue;
-      const int cand = alt_lookup(akeys + (int64_t)(j - 1) * (amask + 1),
-                                  avals + (int64_t)(j - 1) * (amask + 1), amask, key);
-      if (cand < 0) continue;
+      const int cand = alt_lookup(akeys + (int64_t)j * (amask + 1),
+                                  avals + (int64_t)j * (amask + 1), amask, key);
+      if (cand < 0 || cand == c) continue;
       const int dc = xor_popcount(r, cons + (int64_t)cand * Kw, Kw, lane);
       if (dc < d || (dc == d && cand < c)) {
         d = dc;
         c = cand;
       }
     }
-  } else if (c >= 0) {
-    d = xor_popcount(r, cons + (int64_t)c * Kw, Kw, lane);
   }
   if (c >= 0 && d >= n) c = -1;
   if (lane == 0) {
@@ -404,8 +431,8 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
     const size_t q_csize = take2(sizeof(int32_t) * ncl);
     const size_t q_csig = take2(sizeof(uint32_t) * ncl * H);
     const size_t q_cnnz = take2(sizeof(int32_t) * ncl);
-    const size_t q_akeys = take2(sizeof(uint32_t) * asize * (H > 1 ? H - 1 : 1));
-    const size_t q_avals = take2(sizeof(int32_t) * asize * (H > 1 ? H - 1 : 1));
+    const size_t q_akeys = take2(sizeof(uint32_t) * asize * H);
+    const size_t q_avals = take2(sizeof(int32_t) * asize * H);
     DevBuf t2;
     BSP_TRY(t2.alloc(off2));
     char* T2 = static_cast<char*>(t2.p);
@@ -416,8 +443,8 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
     uint32_t* akeys = (uint32_t*)(T2 + q_akeys);
     int32_t* avals = (int32_t*)(T2 + q_avals);
     BSP_CUDA(cudaMemsetAsync(counts, 0, sizeof(int32_t) * ncl * K, s));
-    BSP_CUDA(cudaMemsetAsync(akeys, 0xff, sizeof(uint32_t) * asize * (H > 1 ? H - 1 : 1), s));
-    BSP_CUDA(cudaMemsetAsync(avals, 0x7f, sizeof(int32_t) * asize * (H > 1 ? H - 1 : 1), s));
+    BSP_CUDA(cudaMemsetAsync(akeys, 0xff, sizeof(uint32_t) * asize * H, s));
+    BSP_CUDA(cudaMemsetAsync(avals, 0x7f, sizeof(int32_t) * asize * H, s));
     k_assign<<<tgrid, 256, 0, s>>>(slot, cnt, lead, cid, M, min_rows, plan->row_cluster, csize);
     k_count_bits<<<(unsigned)ceil_div(M * Kw, 256), 256, 0, s>>>(words, M, Kw, K, plan->row_cluster,
                                                                  counts);
@@ -425,8 +452,8 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
                                                                  plan->cons);
     k_signatures<<<(unsigned)ceil_div(ncl, 8), 256, 0, s>>>(plan->cons, ncl, Kw, H, prm->seed,
                                                             csig, cnnz);
-    if (H > 1)
-      k_alt_insert<<<(unsigned)ceil_div(ncl * (H - 1), 256), 256, 0, s>>>(csig, ncl, H, akeys,
+    if (H >= 2)
+      k_alt_insert<<<(unsigned)ceil_div(ncl * (H / 2), 256), 256, 0, s>>>(csig, ncl, H, akeys,
                                                                         avals, asize - 1);
     k_finalize_rows<<<wgrid, 256, 0, s>>>(words, M, Kw, H, sig, nnz, plan->cons, ncl, akeys, avals,
                                           asize - 1, plan->row_cluster, dcnt, stats);
