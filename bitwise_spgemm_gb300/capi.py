@@ -62,6 +62,7 @@ SIGNATURES = {
     "bsp_plan_get_info": [_P, C.POINTER(PlanInfo)],
     "bsp_spmm_workspace": [_P, _I64, C.POINTER(_SZ)],
     "bsp_spmm": [_P, _I64, _I64, _P, _I, _I64, _I64, _P, _I64, _P, _P, _SZ, _P],
+    "bsp_device_status": [C.POINTER(_I), _I],
 }
 _RESTYPES = {"bsp_status_string": C.c_char_p}
 
@@ -96,3 +97,10 @@ def call(name, *args):
     if st != BSP_OK:
         raise BspError(st, name)
     return st
+
+
+def device_status(clear=True):
+    """Device error word of the asynchronous kernels (0 = none)."""
+    v = C.c_int(0)
+    call("bsp_device_status", C.byref(v), int(clear))
+    return v.value

@@ -3,6 +3,7 @@
 // returns a bsp_status and never aborts (the reference's CHECK_* macros
 // printed and returned EXIT_FAILURE, source/src/common.h:37-55).
 #include <climits>
+#include <cstdlib>
 #include <new>
 
 #include "bsp_internal.cuh"
@@ -213,6 +214,17 @@ int bsp_plan_get_info(const bsp_plan* plan, bsp_plan_info* info) {
 
 static int64_t proto_ldp(int64_t N) { return (N + 7) / 8 * 8; }
 
+// Kernel variant of the TMA-staged prototype path; BSP_BULK_VARIANT selects
+// another (warps, stages, slots) shape, -1 disables the path (tuning only).
+static int bulk_variant() {
+  static int v = -2;
+  if (v == -2) {
+    const char* e = getenv("BSP_BULK_VARIANT");
+    v = e ? atoi(e) : 0;
+  }
+  return v;
+}
+
 int bsp_spmm_workspace(const bsp_plan* plan, int64_t N, size_t* bytes) {
   if (!bytes || N < 0) return BSP_ERR_INVALID_ARG;
   *bytes = 0;
@@ -265,9 +277,26 @@ int bsp_spmm(const uint32_t* A_words, int64_t M, int64_t K, const void* B, int b
     a.n_proto = plan->n_proto;
     a.P = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255));
     a.ldp = proto_ldp(N);
+    a.n_delta = plan->delta_nnz;
     BSP_TRY(launch_proto_sums(a, s));
+    if (K < (int64_t)1 << 30 && bulk_variant() >= 0) {
+      // clustered rows: TMA-staged slices; rows without a cluster: walk A
+      BSP_TRY(launch_spmm_proto_bulk(a, bulk_variant(), s));
+      if (plan->direct_rows > 0) {
+        SpmmArgs d = a;
+        d.row_list = plan->direct_list;
+        d.n_list = plan->direct_rows;
+        BSP_TRY(launch_spmm_rows(d, false, vec, s));
+      }
+      return BSP_OK;
+    }
   }
   return launch_spmm_rows(a, proto, vec, s);
+}
+
+int bsp_device_status(int* status, int clear) {
+  if (!status) return BSP_ERR_INVALID_ARG;
+  return bulk_device_error(status, clear != 0);
 }
 
 }  // extern "C"

@@ -323,6 +323,17 @@ __global__ void __launch_bounds__(256) k_delta_fill(const uint32_t* __restrict__
   }
 }
 
+__global__ void k_direct_flags(const int32_t* __restrict__ cluster, int64_t M, int32_t* __restrict__ flag) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r < M) flag[r] = cluster[r] < 0 ? 1 : 0;
+}
+
+__global__ void k_direct_scatter(const int32_t* __restrict__ flag, const int32_t* __restrict__ pos,
+                                 int64_t M, int32_t* __restrict__ list) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r < M && flag[r]) list[pos[r]] = (int32_t)r;
+}
+
 uint32_t pow2_at_least(int64_t n) {
   uint32_t p = 1024;
   while ((int64_t)p < n && p < 0x80000000u) p <<= 1;
@@ -414,6 +425,7 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
   const size_t p_cl = ptake(sizeof(int32_t) * M);
   const size_t p_dp = ptake(sizeof(int32_t) * (M + 1));
   const size_t p_cons = ptake(sizeof(uint32_t) * ncl * Kw);
+  const size_t p_dl = ptake(sizeof(int32_t) * M);
   void* parena = nullptr;
   BSP_CUDA(cudaMalloc(&parena, poff ? poff : 16));
   plan->arena = parena;
@@ -421,6 +433,7 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
   plan->row_cluster = (int32_t*)(Pa + p_cl);
   plan->delta_ptr = (int32_t*)(Pa + p_dp);
   plan->cons = (uint32_t*)(Pa + p_cons);
+  plan->direct_list = (int32_t*)(Pa + p_dl);
   plan->n_proto = ncl;
 
   if (ncl > 0) {
@@ -487,6 +500,12 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
   if (mode == BSP_PLAN_AUTO) mode = (ncl > 0 && proto_cost < 0.6 * direct_cost) ? BSP_PLAN_PROTO : BSP_PLAN_DIRECT;
   if (ncl == 0) mode = BSP_PLAN_DIRECT;
   plan->mode = mode;
+  if (mode == BSP_PLAN_PROTO && plan->direct_rows > 0) {
+    k_direct_flags<<<tgrid, 256, 0, s>>>(plan->row_cluster, M, flag);
+    BSP_TRY(launch_scan_i32(flag, M, cid, scanws, s));
+    k_direct_scatter<<<tgrid, 256, 0, s>>>(flag, cid, M, plan->direct_list);
+    BSP_LAUNCHED();
+  }
   if (mode == BSP_PLAN_PROTO && plan->delta_nnz > 0) {
     BSP_CUDA(cudaMalloc(&plan->delta_arena, sizeof(uint32_t) * plan->delta_nnz));
     plan->delta_idx = (uint32_t*)plan->delta_arena;

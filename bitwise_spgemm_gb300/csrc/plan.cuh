@@ -14,6 +14,7 @@ struct bsp_plan {
   int32_t* delta_ptr = nullptr;
   uint32_t* delta_idx = nullptr;
   uint32_t* cons = nullptr;
+  int32_t* direct_list = nullptr;  // rows without a cluster (ascending), direct_rows entries
 };
 
 namespace bsp {

@@ -16,14 +16,25 @@ struct SpmmArgs {
   const int32_t* row_cluster;  // [M], -1 = walk A's row
   const int32_t* delta_ptr;    // [M+1]
   const uint32_t* delta_idx;   // column | 0x80000000 for "subtract"
+  int64_t n_delta;             // entries in delta_idx
   const uint32_t* cons;        // [n_proto][Kw] prototype masks
   int64_t n_proto;
   float* P;                    // [n_proto][ldp] prototype sums (workspace)
   int64_t ldp;
+  // optional row subset for the walking kernel (rows of A without a cluster)
+  const int32_t* row_list;     // [n_list] or nullptr = rows 0..M-1
+  int64_t n_list;
 };
 
 // vec = B/C layouts allow 16-byte vector access (else lane-per-column path)
 int launch_spmm_rows(const SpmmArgs& a, bool proto, bool vec, cudaStream_t s);
 int launch_proto_sums(const SpmmArgs& a, cudaStream_t s);
+
+// Prototype rows through TMA bulk copies staged in shared memory
+// (spmm_bulk.cu).  Needs the vector layout; rows without a cluster are
+// skipped (walk them with launch_spmm_rows over the plan's direct-row list).
+int launch_spmm_proto_bulk(const SpmmArgs& a, int variant, cudaStream_t s);
+// Device-side error word of the bulk kernels (0 = none); clear resets it.
+int bulk_device_error(int* out, bool clear);
 
 }  // namespace bsp

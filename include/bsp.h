@@ -213,6 +213,12 @@ int bsp_spmm(const uint32_t* A_words, int64_t M, int64_t K, const void* B,
              const bsp_plan* plan, void* workspace, size_t workspace_bytes,
              bsp_stream_t stream);
 
+/* Device-side status of the asynchronous kernels (0 = none; 1 = a bounded
+ * mbarrier wait of the TMA-staged SpMM expired and its output is invalid).
+ * Synchronises the device; clear != 0 resets the word.  No reference
+ * counterpart (the reference has no device-side error reporting).         */
+int bsp_device_status(int* status, int clear);
+
 #ifdef __cplusplus
 }
 #endif

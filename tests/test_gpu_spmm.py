@@ -196,3 +196,37 @@ def test_clustered_small_plans_all_modes():
     plan = ops.Plan(wd, 2048, mode=capi.PLAN_PROTO)
     C = ops.spmm(wd, 2048, bf16_dev(b16), plan=plan).cpu().numpy()
     _check_f64(C, words, 2048, W.bf16_bits_to_f32(b16))
+
+
+@pytest.mark.parametrize("N", [8, 520, 1536, 2056])
+@pytest.mark.parametrize("bdt", ["f32", "bf16", "f16"])
+def test_proto_bulk_mixed_rows(N, bdt):
+    """Clustered rows (TMA-staged prototype path) mixed with random rows (walked
+    directly), several column chunks including a ragged last one."""
+    rng = np.random.default_rng(N)
+    A, _, _ = W.clustered_bits(1200, 3000, n_proto=6, p_proto=0.08, p_flip=0.004, seed_proto=N,
+                               seed_rows=N + 1)
+    A[::17] = rng.random((A[::17].shape[0], 3000)) < 0.05  # rows that fit no cluster
+    words = W.pack_bits(A)
+    wd = words_dev(words)
+    Bf = rng.standard_normal((3000, N)).astype(np.float32)
+    if bdt == "bf16":
+        b16 = W.f32_to_bf16_bits(Bf)
+        Bf = W.bf16_bits_to_f32(b16)
+        B = bf16_dev(b16)
+    elif bdt == "f16":
+        B = torch.from_numpy(Bf).half().cuda()
+        Bf = B.float().cpu().numpy()
+    else:
+        B = torch.from_numpy(Bf).cuda()
+    plan = ops.Plan(wd, 3000, mode=capi.PLAN_PROTO)
+    info = plan.info()
+    assert info["mode"] == capi.PLAN_PROTO and info["direct_rows"] > 0
+    C = ops.spmm(wd, 3000, B, plan=plan).cpu().numpy()
+    assert capi.device_status() == 0
+    _check_f64(C, words, 3000, Bf)
+    # integer-valued B: the bulk path is exact
+    Bi = rng.integers(-8, 9, (3000, N)).astype(np.float32)
+    Ci = ops.spmm(wd, 3000, torch.from_numpy(Bi).cuda(), plan=plan).cpu().numpy()
+    assert np.array_equal(Ci.astype(np.float64), O.spmm_f64(words, 3000, Bi))
+    assert capi.device_status() == 0
