@@ -214,14 +214,24 @@ int bsp_plan_get_info(const bsp_plan* plan, bsp_plan_info* info) {
 
 static int64_t proto_ldp(int64_t N) { return (N + 7) / 8 * 8; }
 
-// Kernel variant of the TMA-staged prototype path; BSP_BULK_VARIANT selects
-// another (warps, stages, slots) shape, -1 disables the path (tuning only).
-static int bulk_variant() {
-  static int v = -2;
-  if (v == -2) {
-    const char* e = getenv("BSP_BULK_VARIANT");
-    v = e ? atoi(e) : 0;
+// Kernel shape of the prototype path: BSP_PROTO_PATH = "bulk" (TMA-staged
+// slices) or "regs" (register gathers), BSP_PROTO_VARIANT its shape index.
+// Defaults come from measurement on GB300; the variables exist for tuning.
+static int env_int(const char* name, int dflt) {
+  const char* e = getenv(name);
+  return e ? atoi(e) : dflt;
+}
+static int proto_path() {
+  static int v = -1;
+  if (v < 0) {
+    const char* e = getenv("BSP_PROTO_PATH");
+    v = (e && e[0] == 'b') ? 1 : 0;  // 1 = bulk, 0 = regs
   }
+  return v;
+}
+static int proto_variant() {
+  static int v = -1000;
+  if (v == -1000) v = env_int("BSP_PROTO_VARIANT", 0);
   return v;
 }
 
@@ -279,9 +289,11 @@ int bsp_spmm(const uint32_t* A_words, int64_t M, int64_t K, const void* B, int b
     a.ldp = proto_ldp(N);
     a.n_delta = plan->delta_nnz;
     BSP_TRY(launch_proto_sums(a, s));
-    if (K < (int64_t)1 << 30 && bulk_variant() >= 0) {
-      // clustered rows: TMA-staged slices; rows without a cluster: walk A
-      BSP_TRY(launch_spmm_proto_bulk(a, bulk_variant(), s));
+    if (K < (int64_t)1 << 30) {
+      // clustered rows: TMA-staged slices or register gathers; rows without
+      // a cluster: walk A
+      if (proto_path() == 1) BSP_TRY(launch_spmm_proto_bulk(a, proto_variant(), s));
+      else BSP_TRY(launch_spmm_proto_regs(a, proto_variant(), s));
       if (plan->direct_rows > 0) {
         SpmmArgs d = a;
         d.row_list = plan->direct_list;

@@ -14,6 +14,7 @@
 //   C[i] = P[c] + Σ_{k ∈ A_i \ cons_c} B[k] − Σ_{k ∈ cons_c \ A_i} B[k],
 // where P[c] = Σ_{k ∈ cons_c} B[k] is computed once per cluster by
 // k_proto_sums (K split across the warps of a CTA, fixed-order reduction).
+#include "ptx.cuh"
 #include "spmm_dev.cuh"
 
 namespace bsp {
@@ -82,6 +83,41 @@ __global__ void __launch_bounds__(256) k_spmm_rows(SpmmArgs a) {
   }
 }
 
+// Prototype rows, register path: one warp per (clustered row, column chunk).
+// The delta gathers are issued first; P[c] is read after griddep_wait(), so
+// with programmatic dependent launch the whole gather phase overlaps the
+// prototype-sum kernel.  MINB caps registers (occupancy sweep).
+template <typename BT, int VPL, int D, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_spmm_proto_regs(SpmmArgs a) {
+  using V = Vec<BT>;
+  constexpr int COLS = V::COLS;
+  constexpr int CW = 32 * VPL * COLS;
+  const int lane = threadIdx.x & 31;
+  const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const bool live = row < a.M;
+  const int cl = live ? __ldg(a.row_cluster + row) : -1;
+  if (cl >= 0) {
+    const int n0 = (int)blockIdx.y * CW;
+    const BT* __restrict__ B = static_cast<const BT*>(a.B);
+    int col[VPL];
+    bool cvalid[VPL];
+#pragma unroll
+    for (int v = 0; v < VPL; v++) {
+      col[v] = n0 + (v * 32 + lane) * COLS;
+      cvalid[v] = col[v] < a.N;
+    }
+    ListWalker wk;
+    wk.init(a.delta_idx, __ldg(a.delta_ptr + row), __ldg(a.delta_ptr + row + 1), lane);
+    Acc<VPL, COLS, false> acc;
+    acc.zero();
+    accumulate_walk<BT, VPL, D, false>(wk, B, a.ldb, col, cvalid, acc);
+    ptx::griddep_wait();
+    store_vecs<VPL, COLS, false>(a.C + row * a.ldc, col, cvalid, acc, a.P + (int64_t)cl * a.ldp);
+  } else {
+    ptx::griddep_wait();
+  }
+}
+
 // Scalar fallback for unaligned or ragged layouts: lane = column.
 template <typename BT>
 __global__ void __launch_bounds__(256) k_spmm_rows_scalar(SpmmArgs a) {
@@ -126,6 +162,7 @@ __global__ void __launch_bounds__(512) k_proto_sums(SpmmArgs a) {
   const BT* __restrict__ B = static_cast<const BT*>(a.B);
   int col[1] = {(int)n0 + lane * COLS};
   bool cvalid[1] = {col[0] < a.N};
+  ptx::griddep_launch_dependents();
   const uint32_t* cw = a.cons + c * a.Kw;
   const int w0 = (int)(a.Kw * wid / W), w1 = (int)(a.Kw * (wid + 1) / W);
   BitWalker wk;
@@ -175,6 +212,38 @@ int launch_rows_t(const SpmmArgs& a, bool proto, bool vec, cudaStream_t s) {
   return BSP_OK;
 }
 
+template <typename BT, int VPL, int D, int MINB>
+int launch_proto_regs_t(const SpmmArgs& a, cudaStream_t s) {
+  constexpr int CW = 32 * VPL * Vec<BT>::COLS;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)ceil_div(a.M, 8), (unsigned)ceil_div(a.N, CW));
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  BSP_CUDA(cudaLaunchKernelEx(&cfg, k_spmm_proto_regs<BT, VPL, D, MINB>, a));
+  return BSP_OK;
+}
+
+template <typename BT>
+int launch_proto_regs_v(const SpmmArgs& a, int variant, cudaStream_t s) {
+  constexpr bool F32 = Vec<BT>::COLS == 4;
+  // variants: columns per warp (VPL vectors per lane), gathers in flight (D), min blocks/SM
+  if (a.N <= 32 * Vec<BT>::COLS) return launch_proto_regs_t<BT, 1, 16, 3>(a, s);
+  switch (variant) {
+    case 1: return launch_proto_regs_t<BT, 2, 4, 4>(a, s);
+    case 2: return launch_proto_regs_t<BT, 2, 8, 3>(a, s);
+    case 3: return launch_proto_regs_t<BT, 1, 8, 4>(a, s);
+    case 4: return launch_proto_regs_t<BT, 1, 16, 3>(a, s);
+    case 5: return launch_proto_regs_t<BT, (F32 ? 4 : 2), 4, 2>(a, s);
+    default: return launch_proto_regs_t<BT, (F32 ? 4 : 2), 2, 4>(a, s);
+  }
+}
+
 template <typename BT>
 int launch_proto_t(const SpmmArgs& a, cudaStream_t s) {
   constexpr int CW = 32 * Vec<BT>::COLS;
@@ -194,6 +263,16 @@ int launch_spmm_rows(const SpmmArgs& a, bool proto, bool vec, cudaStream_t s) {
     case BSP_F32: return launch_rows_t<float>(a, proto, vec, s);
     case BSP_BF16: return launch_rows_t<__nv_bfloat16>(a, proto, vec, s);
     case BSP_F16: return launch_rows_t<__half>(a, proto, vec, s);
+    default: return BSP_ERR_UNSUPPORTED;
+  }
+}
+
+int launch_spmm_proto_regs(const SpmmArgs& a, int variant, cudaStream_t s) {
+  if (a.M == 0 || a.N == 0) return BSP_OK;
+  switch (a.bdt) {
+    case BSP_F32: return launch_proto_regs_v<float>(a, variant, s);
+    case BSP_BF16: return launch_proto_regs_v<__nv_bfloat16>(a, variant, s);
+    case BSP_F16: return launch_proto_regs_v<__half>(a, variant, s);
     default: return BSP_ERR_UNSUPPORTED;
   }
 }

@@ -29,6 +29,9 @@ struct SpmmArgs {
 // vec = B/C layouts allow 16-byte vector access (else lane-per-column path)
 int launch_spmm_rows(const SpmmArgs& a, bool proto, bool vec, cudaStream_t s);
 int launch_proto_sums(const SpmmArgs& a, cudaStream_t s);
+// Clustered rows through registers, launched as a programmatic dependent of
+// the prototype-sum kernel; rows without a cluster are left to the walker.
+int launch_spmm_proto_regs(const SpmmArgs& a, int variant, cudaStream_t s);
 
 // Prototype rows through TMA bulk copies staged in shared memory
 // (spmm_bulk.cu).  Needs the vector layout; rows without a cluster are

@@ -259,6 +259,9 @@ int launch_bulk_variant(const SpmmArgs& a, int n_delta, int variant, cudaStream_
     case 2: return launch_bulk_t<BT, 4, 3, 9>(a, n_delta, st);
     case 3: return launch_bulk_t<BT, 8, 2, 6>(a, n_delta, st);
     case 4: return launch_bulk_t<BT, 6, 4, 4>(a, n_delta, st);
+    case 5: return launch_bulk_t<BT, 16, 2, 3>(a, n_delta, st);
+    case 6: return launch_bulk_t<BT, 12, 2, 4>(a, n_delta, st);
+    case 7: return launch_bulk_t<BT, 10, 2, 5>(a, n_delta, st);
     default: return launch_bulk_t<BT, 6, 3, 6>(a, n_delta, st);
   }
 }
