@@ -55,14 +55,14 @@ __global__ void __launch_bounds__(kPsWarps * 32) k_proto_stream(SpmmArgs a, cons
                                               (size_t)kPsProtos * CW * sizeof(float));
   ptx::griddep_launch_dependents();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t k0 = (int64_t)blockIdx.x * R;
+  const int64_t k0 = min((int64_t)blockIdx.x * R, a.K);
   const int64_t k1 = min(a.K, k0 + R);
   const int n0 = (int)blockIdx.y * CW;
   const int ncols = min(CW, (int)(a.N - n0));
   const int c0 = (int)blockIdx.z * kPsProtos;
   const int nprot = min(kPsProtos, (int)(a.n_proto - c0));
   const uint32_t row_bytes = (uint32_t)ncols * sizeof(BT);
-  const int nrows = (int)(k1 - k0);
+  const int nrows = (int)(k1 - k0);  // 0 ≤ nrows ≤ R ≤ kPsMaxRows (host guarantees nrows ≥ 1)
   if (threadIdx.x == 0) {
     ptx::mbar_init(bar, 1);
     ptx::fence_mbar_init();
@@ -372,17 +372,21 @@ int launch_rows_stream_v(const SpmmArgs& a, int variant, cudaStream_t s) {
 
 }  // namespace
 
+// Blocks of the prototype-sum stream: R rows of B per CTA, R ≤ kPsMaxRows
+// (shared memory: R*512 B staged rows + 64*CW*4 B partial sums), and about
+// one CTA per SM.  G = ceil(K/R), so every CTA gets 1..R rows — the byte
+// count each CTA announces to its mbarrier is R*512 ≤ 160 KB, inside the
+// 2^20-1 limit of mbarrier.expect_tx.
 size_t proto_stream_partial_bytes(int64_t K, int64_t n_proto, int64_t ldp, int* G, int* rows_per_block) {
-  // rows per CTA bounded by shared memory: R*CW*esize + 64*CW*4 ≤ 224 KB with
-  // CW*esize = 512 bytes (FP32) or 512 bytes (16-bit) per staged row
-  const int R = 320;
-  int g = (int)ceil_div(K, R);
-  const int want = num_sms();
-  if (g < want) g = want;
-  if (g > K) g = (int)K;
+  constexpr int64_t kPsMaxRows = 320;
+  int64_t g = ceil_div(K, kPsMaxRows);
+  if (g < num_sms()) g = num_sms();
+  if (g > K) g = K;
   if (g < 1) g = 1;
-  *G = g;
-  *rows_per_block = (int)ceil_div(K, g);
+  const int64_t R = ceil_div(K, g);
+  g = ceil_div(K, R);
+  *G = (int)g;
+  *rows_per_block = (int)R;
   return sizeof(float) * (size_t)g * (size_t)n_proto * (size_t)ldp;
 }
 
