@@ -221,17 +221,17 @@ static int env_int(const char* name, int dflt) {
   const char* e = getenv(name);
   return e ? atoi(e) : dflt;
 }
-static int proto_path() {  // 0 = stream (default), 1 = bulk, 2 = regs
+static int proto_path() {  // 0 = register gathers (default), 1 = TMA-staged slices
   static int v = -1;
   if (v < 0) {
     const char* e = getenv("BSP_PROTO_PATH");
-    v = (e && e[0] == 'b') ? 1 : (e && e[0] == 'r') ? 2 : 0;
+    v = (e && e[0] == 'b') ? 1 : 0;
   }
   return v;
 }
 static int proto_variant() {
   static int v = -1000;
-  if (v == -1000) v = env_int("BSP_PROTO_VARIANT", 0);
+  if (v == -1000) v = env_int("BSP_PROTO_VARIANT", proto_path() == 1 ? 3 : 1);
   return v;
 }
 
@@ -239,10 +239,7 @@ int bsp_spmm_workspace(const bsp_plan* plan, int64_t N, size_t* bytes) {
   if (!bytes || N < 0) return BSP_ERR_INVALID_ARG;
   *bytes = 0;
   if (plan && plan->mode == BSP_PLAN_PROTO) {
-    int G = 0, R = 0;
-    const size_t p = sizeof(float) * (size_t)plan->n_proto * (size_t)proto_ldp(N);
-    const size_t part = proto_stream_partial_bytes(plan->K, plan->n_proto, proto_ldp(N), &G, &R);
-    *bytes = ((p + 255) & ~size_t(255)) + part + 512;
+    *bytes = sizeof(float) * (size_t)plan->n_proto * (size_t)proto_ldp(N) + 256;
   }
   return BSP_OK;
 }
@@ -292,19 +289,12 @@ int bsp_spmm(const uint32_t* A_words, int64_t M, int64_t K, const void* B, int b
     a.P = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255));
     a.ldp = proto_ldp(N);
     a.n_delta = plan->delta_nnz;
-    float* partial = reinterpret_cast<float*>(
-        reinterpret_cast<char*>(a.P) + ((sizeof(float) * (size_t)a.n_proto * (size_t)a.ldp + 255) & ~size_t(255)));
     if (K < (int64_t)1 << 30) {
-      // prototype sums, then clustered rows (streamed, TMA-staged or register
-      // gathers); rows without a cluster: walk A
-      if (proto_path() == 0) {
-        BSP_TRY(launch_proto_sums_stream(a, plan->consT, (int)ceil_div(plan->n_proto, 32), partial, s));
-        BSP_TRY(launch_spmm_proto_stream(a, proto_variant(), s));
-      } else {
-        BSP_TRY(launch_proto_sums(a, s));
-        if (proto_path() == 1) BSP_TRY(launch_spmm_proto_bulk(a, proto_variant(), s));
-        else BSP_TRY(launch_spmm_proto_regs(a, proto_variant(), s));
-      }
+      // prototype sums, then clustered rows (register gathers, or slices
+      // staged by TMA bulk copies); rows without a cluster: walk A
+      BSP_TRY(launch_proto_sums(a, s));
+      if (proto_path() == 1) BSP_TRY(launch_spmm_proto_bulk(a, proto_variant(), s));
+      else BSP_TRY(launch_spmm_proto_regs(a, proto_variant(), s));
       if (plan->direct_rows > 0) {
         SpmmArgs d = a;
         d.row_list = plan->direct_list;
@@ -320,11 +310,7 @@ int bsp_spmm(const uint32_t* A_words, int64_t M, int64_t K, const void* B, int b
 
 int bsp_device_status(int* status, int clear) {
   if (!status) return BSP_ERR_INVALID_ARG;
-  int a = 0, b = 0;
-  BSP_TRY(bulk_device_error(&a, clear != 0));
-  BSP_TRY(stream_device_error(&b, clear != 0));
-  *status = a ? a : b;
-  return BSP_OK;
+  return bulk_device_error(status, clear != 0);
 }
 
 }  // extern "C"

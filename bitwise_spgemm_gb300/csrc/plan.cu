@@ -426,7 +426,6 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
   const size_t p_dp = ptake(sizeof(int32_t) * (M + 1));
   const size_t p_cons = ptake(sizeof(uint32_t) * ncl * Kw);
   const size_t p_dl = ptake(sizeof(int32_t) * M);
-  const size_t p_ct = ptake(sizeof(uint32_t) * K * ceil_div(ncl, 32));
   void* parena = nullptr;
   BSP_CUDA(cudaMalloc(&parena, poff ? poff : 16));
   plan->arena = parena;
@@ -435,7 +434,6 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
   plan->delta_ptr = (int32_t*)(Pa + p_dp);
   plan->cons = (uint32_t*)(Pa + p_cons);
   plan->direct_list = (int32_t*)(Pa + p_dl);
-  plan->consT = (uint32_t*)(Pa + p_ct);
   plan->n_proto = ncl;
 
   if (ncl > 0) {
@@ -502,7 +500,6 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
   if (mode == BSP_PLAN_AUTO) mode = (ncl > 0 && proto_cost < 0.6 * direct_cost) ? BSP_PLAN_PROTO : BSP_PLAN_DIRECT;
   if (ncl == 0) mode = BSP_PLAN_DIRECT;
   plan->mode = mode;
-  if (mode == BSP_PLAN_PROTO) BSP_TRY(launch_transpose_bits(plan->cons, ncl, K, plan->consT, s));
   if (mode == BSP_PLAN_PROTO && plan->direct_rows > 0) {
     k_direct_flags<<<tgrid, 256, 0, s>>>(plan->row_cluster, M, flag);
     BSP_TRY(launch_scan_i32(flag, M, cid, scanws, s));

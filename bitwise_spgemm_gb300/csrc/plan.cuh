@@ -15,7 +15,6 @@ struct bsp_plan {
   uint32_t* delta_idx = nullptr;
   uint32_t* cons = nullptr;
   int32_t* direct_list = nullptr;  // rows without a cluster (ascending), direct_rows entries
-  uint32_t* consT = nullptr;       // prototype masks transposed: [K][ceil(n_proto/32)]
 };
 
 namespace bsp {

@@ -236,10 +236,11 @@ int launch_proto_regs_v(const SpmmArgs& a, int variant, cudaStream_t s) {
   if (a.N <= 32 * Vec<BT>::COLS) return launch_proto_regs_t<BT, 1, 16, 3>(a, s);
   switch (variant) {
     case 1: return launch_proto_regs_t<BT, 2, 4, 4>(a, s);
-    case 2: return launch_proto_regs_t<BT, 2, 8, 3>(a, s);
-    case 3: return launch_proto_regs_t<BT, 1, 8, 4>(a, s);
-    case 4: return launch_proto_regs_t<BT, 1, 16, 3>(a, s);
-    case 5: return launch_proto_regs_t<BT, (F32 ? 4 : 2), 4, 2>(a, s);
+    case 2: return launch_proto_regs_t<BT, (F32 ? 4 : 2), 1, 5>(a, s);
+    case 3: return launch_proto_regs_t<BT, 2, 2, 6>(a, s);
+    case 4: return launch_proto_regs_t<BT, 2, 1, 8>(a, s);
+    case 5: return launch_proto_regs_t<BT, 1, 4, 8>(a, s);
+    case 6: return launch_proto_regs_t<BT, 2, 2, 5>(a, s);
     default: return launch_proto_regs_t<BT, (F32 ? 4 : 2), 2, 4>(a, s);
   }
 }

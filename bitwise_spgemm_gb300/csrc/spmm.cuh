@@ -40,13 +40,6 @@ int launch_spmm_proto_bulk(const SpmmArgs& a, int variant, cudaStream_t s);
 // Device-side error word of the bulk kernels (0 = none); clear resets it.
 int bulk_device_error(int* out, bool clear);
 
-// Streaming prototype path (spmm_stream.cu): P = cons·B by streaming B
-// (consT = transposed prototype masks [K][Pw]), then the clustered rows.
-size_t proto_stream_partial_bytes(int64_t K, int64_t n_proto, int64_t ldp, int* G,
-                                  int* rows_per_block);
-int launch_proto_sums_stream(const SpmmArgs& a, const uint32_t* consT, int Pw, float* partial,
-                             cudaStream_t s);
-int launch_spmm_proto_stream(const SpmmArgs& a, int variant, cudaStream_t s);
-int stream_device_error(int* out, bool clear);
+
 
 }  // namespace bsp
