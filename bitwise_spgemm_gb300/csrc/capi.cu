@@ -214,6 +214,20 @@ int bsp_plan_get_info(const bsp_plan* plan, bsp_plan_info* info) {
 
 static int64_t proto_ldp(int64_t N) { return (N + 7) / 8 * 8; }
 
+// Cost model of the tensor-core decision, in seconds: dense BF16 work on the
+// occupied (128 x 32) tiles at ~1.2 PFLOP/s against the B-row gathers of the
+// CUDA-core schedule at ~8 TB/s (rates measured on GB300).
+static bool use_tensor_cores(const bsp_plan* plan, int64_t N, int esize) {
+  const char* e = getenv("BSP_TC");
+  if (e) return e[0] == '1';
+  const double tc = (double)plan->occ_tiles * 128.0 * 32.0 * (double)N * 2.0 / 1.2e15;
+  double gathers = (double)plan->nnz;
+  if (plan->mode == BSP_PLAN_PROTO)
+    gathers = (double)(plan->proto_nnz + plan->delta_nnz + plan->direct_nnz + plan->M);
+  const double cc = gathers * (double)N * (double)esize / 8e12;
+  return tc < cc;
+}
+
 // Kernel shape of the prototype path: BSP_PROTO_PATH = "bulk" (TMA-staged
 // slices) or "regs" (register gathers), BSP_PROTO_VARIANT its shape index.
 // Defaults come from measurement on GB300; the variables exist for tuning.
@@ -276,6 +290,11 @@ int bsp_spmm(const uint32_t* A_words, int64_t M, int64_t K, const void* B, int b
   a.N = N;
   a.C = C;
   a.ldc = ldc;
+  // Tensor cores for 16-bit B when the occupied bit tiles make a dense
+  // contraction cheaper than gathering B rows (BSP_TC=0/1 forces the choice).
+  if (plan && vec && b_dtype != BSP_F32 && N % 8 == 0 && use_tensor_cores(plan, N, esz)) {
+    return launch_spmm_tc(a, plan->occ, s);
+  }
   const bool proto = plan && plan->mode == BSP_PLAN_PROTO && vec;
   if (proto) {
     size_t need = 0;
@@ -310,7 +329,11 @@ int bsp_spmm(const uint32_t* A_words, int64_t M, int64_t K, const void* B, int b
 
 int bsp_device_status(int* status, int clear) {
   if (!status) return BSP_ERR_INVALID_ARG;
-  return bulk_device_error(status, clear != 0);
+  int a = 0, b = 0;
+  BSP_TRY(bulk_device_error(&a, clear != 0));
+  BSP_TRY(tc_device_error(&b, clear != 0));
+  *status = a ? a : b;
+  return BSP_OK;
 }
 
 }  // extern "C"

@@ -15,6 +15,8 @@ struct bsp_plan {
   uint32_t* delta_idx = nullptr;
   uint32_t* cons = nullptr;
   int32_t* direct_list = nullptr;  // rows without a cluster (ascending), direct_rows entries
+  uint32_t* occ = nullptr;         // occupied 32-column K tiles per 128-row block (tensor-core path)
+  int64_t occ_tiles = 0;           // number of occupied (128-row, 32-column) tiles
 };
 
 namespace bsp {

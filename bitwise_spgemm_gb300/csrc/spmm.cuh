@@ -40,6 +40,15 @@ int launch_spmm_proto_bulk(const SpmmArgs& a, int variant, cudaStream_t s);
 // Device-side error word of the bulk kernels (0 = none); clear resets it.
 int bulk_device_error(int* out, bool clear);
 
+// Tensor-core path (spmm_tc.cu) for 16-bit B: occupancy bitmap of 32-column
+// K tiles per 128-row block ([ceil(M/128)][tc_occupancy_words(K)]), then the
+// tcgen05 kernel over the occupied tiles.
+int tc_occupancy_words(int64_t K);
+int launch_tile_occupancy(const uint32_t* A, int64_t M, int64_t K, uint32_t* occ,
+                          unsigned long long* count, cudaStream_t s);
+int launch_spmm_tc(const SpmmArgs& a, const uint32_t* occ, cudaStream_t s);
+int tc_device_error(int* out, bool clear);
+
 
 
 }  // namespace bsp

@@ -1,0 +1,103 @@
+"""tcgen05 tensor-core path (16-bit B): parity with the oracle.
+
+Bit tiles are expanded to exact 0/1 BF16/FP16 operands and products by 1 are
+exact, so integer-valued B must give identical results; for N(0,1) B the
+FP32 accumulation order differs from the oracle's, and every element is
+checked against FP64 relative to its summation scale (≤ 1e-4), well inside
+the 1e-2 bound of the precision form."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import oracle as O
+from bitwise_spgemm_gb300 import capi, ops
+from bitwise_spgemm_gb300 import workloads as W
+from gpu_util import bf16_dev, words_dev
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-4
+
+
+@pytest.fixture
+def force_tc():
+    old = os.environ.get("BSP_TC")
+    os.environ["BSP_TC"] = "1"
+    yield
+    if old is None:
+        del os.environ["BSP_TC"]
+    else:
+        os.environ["BSP_TC"] = old
+
+
+def _b16(Bf, kind):
+    if kind == "bf16":
+        b = W.f32_to_bf16_bits(Bf)
+        return bf16_dev(b), W.bf16_bits_to_f32(b)
+    t = torch.from_numpy(Bf).half().cuda()
+    return t, t.float().cpu().numpy()
+
+
+@pytest.mark.parametrize("kind", ["bf16", "f16"])
+@pytest.mark.parametrize("M,K,N,p", [(128, 32, 256, 0.3), (300, 200, 264, 0.2), (1000, 1000, 512, 0.05),
+                                     (77, 64, 8, 0.5), (512, 2048, 1024, 0.01)])
+def test_tc_random(force_tc, kind, M, K, N, p):
+    rng = np.random.default_rng(M + K + N)
+    bits = rng.random((M, K)) < p
+    bits[: min(M, 130), : min(K, 40)] = False  # an all-empty leading tile region
+    words = W.pack_bits(bits)
+    wd = words_dev(words)
+    plan = ops.Plan(wd, K)
+    Bf = rng.standard_normal((K, N)).astype(np.float32)
+    B, Bexact = _b16(Bf, kind)
+    C = ops.spmm(wd, K, B, plan=plan).cpu().numpy()
+    assert capi.device_status() == 0
+    mx, mean, _ = O.rel_errors(C, O.spmm_f64(words, K, Bexact), O.spmm_abs_f64(words, K, Bexact))
+    assert mx <= TOL, (mx, mean)
+    # integer-valued B: exact
+    Bi = rng.integers(-8, 9, (K, N)).astype(np.float32)
+    Bt, Bie = _b16(Bi, kind)
+    Ci = ops.spmm(wd, K, Bt, plan=plan).cpu().numpy()
+    assert np.array_equal(Ci.astype(np.float64), O.spmm_f64(words, K, Bie))
+
+
+def test_tc_block_structured_sample():
+    """Block-structured A (32x32 tiles present w.p. 0.3, bits 0.8), the
+    tensor-core workload at a reduced size; AUTO dispatch must pick the
+    tensor cores."""
+    A, present = W.block_bits(2048, 4096, p_tile=0.3, p_bit=0.8, seed=5)
+    words = W.pack_bits(A)
+    wd = words_dev(words)
+    plan = ops.Plan(wd, 4096)
+    rng = np.random.default_rng(6)
+    Bf = rng.standard_normal((4096, 768)).astype(np.float32)
+    B, Bexact = _b16(Bf, "bf16")
+    C = ops.spmm(wd, 4096, B, plan=plan).cpu().numpy()
+    assert capi.device_status() == 0
+    mx, _, _ = O.rel_errors(C, O.spmm_f64(words, 4096, Bexact), O.spmm_abs_f64(words, 4096, Bexact))
+    assert mx <= TOL
+    # the CUDA-core walk agrees
+    os.environ["BSP_TC"] = "0"
+    try:
+        C2 = ops.spmm(wd, 4096, B, plan=plan).cpu().numpy()
+    finally:
+        del os.environ["BSP_TC"]
+    assert np.abs(C - C2).max() <= 1e-4 * max(1.0, np.abs(C2).max())
+
+
+@pytest.mark.slow
+def test_config3_full_size_row_sample():
+    cfg = W.config3()
+    words, K, N = cfg["words"], cfg["K"], cfg["N"]
+    wd = words_dev(words)
+    plan = ops.Plan(wd, K)
+    B = bf16_dev(cfg["B"])
+    C = ops.spmm(wd, K, B, plan=plan)
+    assert capi.device_status() == 0
+    Bexact = W.bf16_bits_to_f32(cfg["B"])
+    rows = np.r_[0:128, 8192:8256, 16320:16384]
+    Cs = C[torch.from_numpy(rows).cuda()].cpu().numpy()
+    C64 = O.spmm_f64(words[rows], K, Bexact)
+    mx, _, mxn = O.rel_errors(Cs, C64, O.spmm_abs_f64(words[rows], K, Bexact))
+    assert mx <= TOL and mxn <= 1e-2
