@@ -245,7 +245,7 @@ static int proto_path() {  // 0 = register gathers (default), 1 = TMA-staged sli
 }
 static int proto_variant() {
   static int v = -1000;
-  if (v == -1000) v = env_int("BSP_PROTO_VARIANT", proto_path() == 1 ? 3 : 1);
+  if (v == -1000) v = env_int("BSP_PROTO_VARIANT", proto_path() == 1 ? 3 : 4);
   return v;
 }
 

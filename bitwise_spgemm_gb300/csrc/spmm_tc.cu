@@ -38,7 +38,11 @@ constexpr int kAStage = kTcM * kTcK * 2;  // 8 KB
 constexpr int kBStage = kTcK * kTcN * 2;  // 16 KB
 constexpr int kProducers = 128;
 constexpr int kTcThreads = 160;
-constexpr uint32_t kTmemCols = 256;
+// kGuard: extra shared memory past the stage buffers and a full 512-column
+// TMEM allocation, so that a misread descriptor field cannot reach memory
+// the CTA does not own (first bring-up; costs one CTA per SM).
+constexpr bool kGuard = true;
+constexpr uint32_t kTmemCols = kGuard ? 512 : 256;
 // A (K-major): element (m, k) at (m/8)*512 + (k/8)*128 + (m%8)*16 + (k%8)*2
 constexpr uint32_t kALbo = 128, kASbo = 512;
 // B (MN-major): element (k, n) at (n/8)*512 + (k/8)*128 + (k%8)*16 + (n%8)*2
@@ -52,6 +56,7 @@ struct __align__(1024) TcSmem {
   uint64_t done;
   uint32_t tmem_addr;
   int abort;
+  uint8_t guard[kGuard ? 65536 : 16];
 };
 
 // Instruction descriptor for kind::f16: D f32, A and B of the same 16-bit

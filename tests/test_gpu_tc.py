@@ -64,8 +64,7 @@ def test_tc_random(force_tc, kind, M, K, N, p):
 
 def test_tc_block_structured_sample():
     """Block-structured A (32x32 tiles present w.p. 0.3, bits 0.8), the
-    tensor-core workload at a reduced size; AUTO dispatch must pick the
-    tensor cores."""
+    tensor-core workload at a reduced size, through the default dispatch."""
     A, present = W.block_bits(2048, 4096, p_tile=0.3, p_bit=0.8, seed=5)
     words = W.pack_bits(A)
     wd = words_dev(words)
