@@ -40,13 +40,19 @@ constexpr int kProducers = 128;
 constexpr int kTcThreads = 160;
 // kGuard: extra shared memory past the stage buffers and a full 512-column
 // TMEM allocation, so that a misread descriptor field cannot reach memory
-// the CTA does not own (first bring-up; costs one CTA per SM).
-constexpr bool kGuard = true;
+// the CTA does not own (used for the first bring-up of a descriptor change;
+// costs one CTA per SM).
+constexpr bool kGuard = false;
 constexpr uint32_t kTmemCols = kGuard ? 512 : 256;
-// A (K-major): element (m, k) at (m/8)*512 + (k/8)*128 + (m%8)*16 + (k%8)*2
+// Operands are stored as 8x16-byte core matrices (no swizzle).  In both
+// descriptors the leading byte offset (LBO) is the distance between core
+// matrices adjacent along K and the stride byte offset (SBO) the distance
+// between core matrices adjacent along M (A) or N (B) — measured on GB300
+// with one-hot A rows and position-encoding B values.
+// A (K-major):  element (m, k) at (m/8)*kASbo + (k/8)*kALbo + (m%8)*16 + (k%8)*2
 constexpr uint32_t kALbo = 128, kASbo = 512;
-// B (MN-major): element (k, n) at (n/8)*512 + (k/8)*128 + (k%8)*16 + (n%8)*2
-constexpr uint32_t kBLbo = 512, kBSbo = 128;
+// B (MN-major): element (k, n) at (n/8)*kBSbo + (k/8)*kBLbo + (k%8)*16 + (n%8)*2
+constexpr uint32_t kBLbo = 128, kBSbo = 512;
 
 struct __align__(1024) TcSmem {
   uint8_t a[kStages][kAStage];
@@ -158,7 +164,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(SpmmArgs a, const uin
         const int ncol = n0 + n8 * 8;
         const bool ok = krow < a.K && ncol < a.N;
         const BT* src = ok ? B + krow * a.ldb + ncol : B;
-        ptx::cp_async_16(sm.b[s] + n8 * kBLbo + (k >> 3) * kBSbo + (k & 7) * 16, src, ok ? 16u : 0u);
+        ptx::cp_async_16(sm.b[s] + n8 * kBSbo + (k >> 3) * kBLbo + (k & 7) * 16, src, ok ? 16u : 0u);
       }
       ptx::cp_async_commit();
       // stage i-2 is now complete: publish it to the MMA issuer
@@ -190,7 +196,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(SpmmArgs a, const uin
 #pragma unroll
       for (int j = 0; j < 2; j++) {
         const uint64_t ad = ptx::smem_desc_noswizzle(sm.a[s] + j * 2 * kALbo, kALbo, kASbo);
-        const uint64_t bd = ptx::smem_desc_noswizzle(sm.b[s] + j * 2 * kBSbo, kBLbo, kBSbo);
+        const uint64_t bd = ptx::smem_desc_noswizzle(sm.b[s] + j * 2 * kBLbo, kBLbo, kBSbo);
         ptx::tc_mma_f16(tmem, ad, bd, idesc, (i > 0) || (j > 0));
       }
       ptx::tc_commit(&sm.empty[s]);
