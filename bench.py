@@ -43,6 +43,9 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=10)
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--config", default="c2", choices=["c1", "c2", "c3"],
+                   help="c2 (default): clustered FP32 8192x8192x512; c1: 1024x1024x256 "
+                        "integer B; c3: block-structured 16384x16384x2048 BF16 (tensor cores)")
     return p.parse_args()
 
 
@@ -83,6 +86,15 @@ def peaks():
             d = json.load(f)
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+def tensor_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["bf16_tflops"]), "measured"
+    return 1900.0, "fallback"
 
 
 def traffic_from_profiles():
@@ -359,10 +371,86 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_other(args):
+    """Secondary configurations: c1 (plain small, integer B) and c3 (block-
+    structured, BF16 B on the tensor cores).  Same timing rules: CUDA events
+    on the launching stream around K steps, warm-up first."""
+    import torch
+    from bitwise_spgemm_gb300 import capi, ops
+    from bitwise_spgemm_gb300 import workloads as W
+    ws, rank, local = dist_setup(args)
+    dev = torch.device("cuda", local)
+    cfg = W.config1() if args.config == "c1" else W.config3()
+    M, K, N = cfg["M"], cfg["K"], cfg["N"]
+    words = torch.from_numpy(np.ascontiguousarray(cfg["words"]).view(np.int32)).to(dev)
+    if cfg["b_dtype"] == "bf16":
+        B = torch.from_numpy(np.ascontiguousarray(cfg["B"]).view(np.int16)).to(dev).view(torch.bfloat16)
+        esz, dtype = 2, "bf16"
+    else:
+        B = torch.from_numpy(cfg["B"]).to(dev)
+        esz, dtype = 4, "f32"
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    plan = ops.Plan(words, K)
+    torch.cuda.synchronize()
+    plan_ms = (time.perf_counter() - t0) * 1e3
+    info = plan.info()
+    C = torch.empty(M, N, device=dev)
+    wsp = torch.empty(max(plan.workspace_bytes(N), 16), dtype=torch.uint8, device=dev)
+    comp = M * ((K + 31) // 32) * 4 + K * N * esz + M * N * 4
+    flops = 2.0 * info["nnz"] * N
+
+    def timed(fn, steps, warm):
+        for _ in range(warm):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        cur = torch.cuda.current_stream()
+        e0.record(cur)
+        for _ in range(steps):
+            fn()
+        e1.record(cur)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    step = lambda: ops.spmm(words, K, B, plan=plan, out=C, workspace=wsp)
+    sampler = ClockSampler(local) if rank == 0 else None
+    if sampler:
+        sampler.start()
+    barrier(ws)
+    ms = max_over_ranks(ws, timed(step, args.steps, max(args.warmup, 3)))
+    barrier(ws)
+    clocks = sampler.stop() if sampler else None
+    out = {"metric": METRIC, "value": ws * comp / (ms * 1e-3) / 1e9, "unit": UNIT, "n_gpus": ws,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic (seeded numpy)",
+           "config": {"workload": cfg["name"], "M": M, "K": K, "N": N, "plan_ms": plan_ms,
+                      "nnz": info["nnz"], "l2": "working set %.0f MB" % (comp / 1e6)},
+           "effective_gflops": flops / (ms * 1e-3) / 1e9, "clocks": clocks}
+    if args.config == "c3":
+        occ = info["occ_tiles"]
+        dense = occ * 128 * 32 * N * 2.0
+        tp, tkind = tensor_peak()
+        out["tensor"] = {"issued_tflops": dense / (ms * 1e-3) / 1e12, "peak_tflops": tp,
+                         "frac": dense / (ms * 1e-3) / 1e12 / tp, "peak_source": tkind,
+                         "occupied_tiles": occ}
+        # the same problem in the plain FP32 form (CUDA cores): a few steps
+        Bf = torch.from_numpy(W.bf16_bits_to_f32(cfg["B"])).to(dev)
+        step32 = lambda: ops.spmm(words, K, Bf, plan=plan, out=C, workspace=wsp)
+        ms32 = timed(step32, 2, 1)
+        out["fp32_form_ms"] = ms32
+        out["speedup_vs_fp32_form"] = ms32 / ms
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    plan.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.config != "c2":
+        run_other(args)
     else:
         run_ours(args)
 

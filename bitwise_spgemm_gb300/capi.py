@@ -37,7 +37,7 @@ class PlanParams(C.Structure):
 class PlanInfo(C.Structure):
     _fields_ = [("M", C.c_int64), ("K", C.c_int64), ("nnz", C.c_int64), ("mode", C.c_int),
                 ("n_proto", C.c_int64), ("proto_nnz", C.c_int64), ("delta_nnz", C.c_int64),
-                ("direct_rows", C.c_int64), ("direct_nnz", C.c_int64)]
+                ("direct_rows", C.c_int64), ("direct_nnz", C.c_int64), ("occ_tiles", C.c_int64)]
 
 
 _P = C.c_void_p

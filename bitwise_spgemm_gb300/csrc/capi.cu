@@ -209,6 +209,7 @@ int bsp_plan_get_info(const bsp_plan* plan, bsp_plan_info* info) {
   info->delta_nnz = plan->mode == BSP_PLAN_PROTO ? plan->delta_nnz : 0;
   info->direct_rows = plan->mode == BSP_PLAN_PROTO ? plan->direct_rows : plan->M;
   info->direct_nnz = plan->mode == BSP_PLAN_PROTO ? plan->direct_nnz : plan->nnz;
+  info->occ_tiles = plan->occ_tiles;
   return BSP_OK;
 }
 

@@ -178,6 +178,7 @@ typedef struct bsp_plan_info {
   int64_t delta_nnz;     /* ± delta entries over all prototype rows         */
   int64_t direct_rows;   /* rows without a prototype                        */
   int64_t direct_nnz;    /* set bits of those rows                          */
+  int64_t occ_tiles;     /* (128-row, 32-column) bit tiles holding a set bit */
 } bsp_plan_info;
 
 /* Build a plan for A (packed LSB-first words[M][ceil(K/32)]).  Runs grouping
