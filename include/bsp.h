@@ -214,6 +214,24 @@ int bsp_spmm(const uint32_t* A_words, int64_t M, int64_t K, const void* B,
              const bsp_plan* plan, void* workspace, size_t workspace_bytes,
              bsp_stream_t stream);
 
+/* bsp_spmm without a workspace argument, for callers that may not allocate
+ * device memory when they run the SpMM (plugin callbacks handed only
+ * pointers, code inside CUDA stream capture, processes whose device memory
+ * belongs to another allocator).  The prototype sums that bsp_spmm keeps in
+ * the caller's workspace live in a static device array of 8 MiB inside the
+ * library, held on every GPU that loads the library until the process exits.
+ * Limit: bsp_spmm_workspace(plan, N) must be ≤ 8 MiB (≈ n_proto * N * 4
+ * bytes), else BSP_ERR_CAPACITY.  The first call on a device looks the
+ * array's address up (cudaGetSymbolAddress); make that first call before any
+ * stream capture.  All calls share the one array: calls that overlap on the
+ * GPU (other streams, other host threads) race and must be serialised by the
+ * caller.  The array keeps the last call's contents; nothing in it needs to
+ * start at zero.  No counterpart in the reference.                          */
+int bsp_spmm_noalloc(const uint32_t* A_words, int64_t M, int64_t K,
+                     const void* B, int b_dtype, int64_t ldb, int64_t N,
+                     float* C, int64_t ldc, const bsp_plan* plan,
+                     bsp_stream_t stream);
+
 /* Device-side status of the asynchronous kernels (0 = none; 1 = a bounded
  * mbarrier wait of the TMA-staged SpMM expired and its output is invalid).
  * Synchronises the device; clear != 0 resets the word.  No reference
