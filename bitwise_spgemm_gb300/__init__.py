@@ -10,7 +10,7 @@ __version__ = "0.1.0"
 def __getattr__(name):
     # torch-dependent helpers are imported lazily so ``import bitwise_spgemm_gb300``
     # stays light for tools that only need the C ABI binding.
-    if name in ("ops", "workloads"):
+    if name in ("ops", "workloads", "autograd"):
         import importlib
         return importlib.import_module("." + name, __name__)
     raise AttributeError(name)

@@ -63,6 +63,9 @@ SIGNATURES = {
     "bsp_spmm_workspace": [_P, _I64, C.POINTER(_SZ)],
     "bsp_spmm": [_P, _I64, _I64, _P, _I, _I64, _I64, _P, _I64, _P, _P, _SZ, _P],
     "bsp_device_status": [C.POINTER(_I), _I],
+    "bsp_spmm_t_workspace": [_I64, _I64, C.POINTER(_SZ)],
+    "bsp_spmm_t": [_P, _I64, _I64, _P, _I, _I64, _I64, _P, _I64, _P, _P, _SZ, _P],
+    "bsp_sddmm": [_P, _I64, _I64, _P, _I64, _P, _I64, _I, _I64, _P, _I64, _P, _P],
     "bsp_spmm_noalloc": [_P, _I64, _I64, _P, _I, _I64, _I64, _P, _I64, _P, _P],
 }
 _RESTYPES = {"bsp_status_string": C.c_char_p}

@@ -328,6 +328,90 @@ int bsp_spmm(const uint32_t* A_words, int64_t M, int64_t K, const void* B, int b
   return launch_spmm_rows(a, proto, vec, s);
 }
 
+int bsp_spmm_t_workspace(int64_t M, int64_t K, size_t* bytes) {
+  if (!bytes || M < 0 || K < 0) return BSP_ERR_INVALID_ARG;
+  *bytes = sizeof(uint32_t) * (size_t)K * (size_t)ceil_div(M, 32) + 256;
+  return BSP_OK;
+}
+
+static bool layout16(const void* p, int64_t ld, int esz, int64_t N, int vcols) {
+  return is_aligned(p, 16) && ((ld * esz) % 16 == 0) && (N % vcols == 0);
+}
+
+int bsp_spmm_t(const uint32_t* A_words, int64_t M, int64_t K, const void* G, int g_dtype, int64_t ldg,
+               int64_t N, float* dX, int64_t lddx, const bsp_plan* plan, void* workspace,
+               size_t workspace_bytes, bsp_stream_t stream) {
+  BSP_TRY(check_dims(M, K));
+  if (N < 0 || N > kMaxCols) return BSP_ERR_INVALID_ARG;
+  if (g_dtype != BSP_F32 && g_dtype != BSP_BF16 && g_dtype != BSP_F16) return BSP_ERR_UNSUPPORTED;
+  if (ldg < N || lddx < N) return BSP_ERR_INVALID_ARG;
+  if (plan && (plan->M != M || plan->K != K || plan->device != current_device())) return BSP_ERR_INVALID_ARG;
+  if (K == 0 || N == 0) return BSP_OK;
+  if (!dX || (M > 0 && (!A_words || !G))) return BSP_ERR_INVALID_ARG;
+  const int esz = dtype_size(g_dtype);
+  if (!is_aligned(G, esz) || !is_aligned(dX, 4) || !is_aligned(A_words, 4)) return BSP_ERR_ALIGNMENT;
+  const cudaStream_t s = (cudaStream_t)stream;
+  if (M == 0) {
+    BSP_CUDA(cudaMemset2DAsync(dX, sizeof(float) * lddx, 0, sizeof(float) * N, K, s));
+    return BSP_OK;
+  }
+  const int vcols = g_dtype == BSP_F32 ? 4 : 8;
+  const bool vec = layout16(G, ldg, esz, N, vcols) && layout16(dX, lddx, 4, N, 4);
+  if (plan && vec && g_dtype != BSP_F32) {
+    const char* e = getenv("BSP_TC");
+    const double tc = (double)plan->occT_tiles * 128.0 * 32.0 * (double)N * 2.0 / 1.2e15;
+    const double cc = (double)plan->nnz * (double)N * (double)esz / 8e12;
+    if (e ? e[0] == '1' : tc < cc)
+      return launch_spmm_t_tc(A_words, M, K, G, g_dtype, ldg, N, dX, lddx, plan->occT, s);
+  }
+  // CUDA cores: transpose the bits into the workspace, then walk the rows of Aᵀ
+  size_t need = 0;
+  bsp_spmm_t_workspace(M, K, &need);
+  if (!workspace || workspace_bytes < need) return BSP_ERR_WORKSPACE;
+  uint32_t* At = reinterpret_cast<uint32_t*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255));
+  BSP_TRY(launch_transpose_bits(A_words, M, K, At, s));
+  SpmmArgs a = {};
+  a.A = At;
+  a.M = K;
+  a.K = M;
+  a.Kw = ceil_div(M, 32);
+  a.B = G;
+  a.bdt = g_dtype;
+  a.ldb = ldg;
+  a.N = N;
+  a.C = dX;
+  a.ldc = lddx;
+  return launch_spmm_rows(a, false, vec, s);
+}
+
+int bsp_sddmm(const uint32_t* A_words, int64_t M, int64_t K, const void* G, int64_t ldg, const void* X,
+              int64_t ldx, int dtype, int64_t N, float* dA, int64_t ldda, const bsp_plan* plan,
+              bsp_stream_t stream) {
+  BSP_TRY(check_dims(M, K));
+  if (N < 0 || N > kMaxCols) return BSP_ERR_INVALID_ARG;
+  if (dtype != BSP_F32 && dtype != BSP_BF16 && dtype != BSP_F16) return BSP_ERR_UNSUPPORTED;
+  if (ldg < N || ldx < N || ldda < K) return BSP_ERR_INVALID_ARG;
+  if (plan && (plan->M != M || plan->K != K || plan->device != current_device())) return BSP_ERR_INVALID_ARG;
+  if (M == 0 || K == 0) return BSP_OK;
+  if (!dA || !A_words || (N > 0 && (!G || !X))) return BSP_ERR_INVALID_ARG;
+  const int esz = dtype_size(dtype);
+  if (!is_aligned(G, esz) || !is_aligned(X, esz) || !is_aligned(dA, 4) || !is_aligned(A_words, 4))
+    return BSP_ERR_ALIGNMENT;
+  const cudaStream_t s = (cudaStream_t)stream;
+  const bool tc_ok = dtype != BSP_F32 && N > 0 && layout16(G, ldg, esz, N, 8) && layout16(X, ldx, esz, N, 8) &&
+                     layout16(dA, ldda, 4, K, 8);
+  bool tc = tc_ok;
+  const char* e = getenv("BSP_TC");
+  if (tc_ok && e) tc = e[0] == '1';
+  else if (tc_ok && plan) {  // dense product on the tensor cores vs one dot product per set bit
+    const double dense = (double)M * (double)K * (double)N * 2.0 / 1.2e15;
+    const double cores = (double)plan->nnz * (double)N * ((double)esz / 8e12 + 2.0 / 6e13);
+    tc = dense < cores;
+  }
+  if (tc) return launch_sddmm_tc(A_words, M, K, G, ldg, X, ldx, dtype, N, dA, ldda, s);
+  return launch_sddmm_rows(A_words, M, K, G, ldg, X, ldx, dtype, N, dA, ldda, s);
+}
+
 int bsp_device_status(int* status, int clear) {
   if (!status) return BSP_ERR_INVALID_ARG;
   int a = 0, b = 0;

@@ -428,6 +428,7 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
   const size_t p_cons = ptake(sizeof(uint32_t) * ncl * Kw);
   const size_t p_dl = ptake(sizeof(int32_t) * M);
   const size_t p_occ = ptake(sizeof(uint32_t) * ceil_div(M, 128) * tc_occupancy_words(K));
+  const size_t p_occT = ptake(sizeof(uint32_t) * ceil_div(K, 128) * tc_occupancy_t_words(M));
   void* parena = nullptr;
   BSP_CUDA(cudaMalloc(&parena, poff ? poff : 16));
   plan->arena = parena;
@@ -438,6 +439,8 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
   plan->direct_list = (int32_t*)(Pa + p_dl);
   plan->occ = (uint32_t*)(Pa + p_occ);
   BSP_TRY(launch_tile_occupancy(words, M, K, plan->occ, stats + 5, s));
+  plan->occT = (uint32_t*)(Pa + p_occT);
+  BSP_TRY(launch_tile_occupancy_t(words, M, K, plan->occT, stats + 6, s));
   plan->n_proto = ncl;
 
   if (ncl > 0) {
@@ -494,6 +497,7 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
   plan->direct_nnz = (int64_t)st[3];
   plan->proto_nnz = (int64_t)st[4];
   plan->occ_tiles = (int64_t)st[5];
+  plan->occT_tiles = (int64_t)st[6];
   if (plan->delta_nnz >= INT_MAX) return BSP_ERR_CAPACITY;
 
   // Cost model in gathered rows of B: direct = nnz; proto = prototype bits +

@@ -17,6 +17,8 @@ struct bsp_plan {
   int32_t* direct_list = nullptr;  // rows without a cluster (ascending), direct_rows entries
   uint32_t* occ = nullptr;         // occupied 32-column K tiles per 128-row block (tensor-core path)
   int64_t occ_tiles = 0;           // number of occupied (128-row, 32-column) tiles
+  uint32_t* occT = nullptr;        // occupied 32-row tiles per 128-column block (transposed product)
+  int64_t occT_tiles = 0;
 };
 
 namespace bsp {

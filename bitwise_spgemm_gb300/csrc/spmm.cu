@@ -256,7 +256,49 @@ int launch_proto_t(const SpmmArgs& a, cudaStream_t s) {
   return BSP_OK;
 }
 
+// SDDMM on CUDA cores: warp per row i of A; the row of dA is zeroed, then for
+// every set bit k (ascending) the lanes stride over N accumulating
+// G[i][j]·X[k][j] in FP32 and a warp reduction writes dA[i][k].
+template <typename T>
+__global__ void __launch_bounds__(256) k_sddmm_rows(const uint32_t* __restrict__ A, int64_t M, int64_t K,
+                                                    int64_t Kw, const T* __restrict__ G, int64_t ldg,
+                                                    const T* __restrict__ X, int64_t ldx, int64_t N,
+                                                    float* __restrict__ dA, int64_t ldda) {
+  const int lane = threadIdx.x & 31;
+  const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (row >= M) return;
+  float* out = dA + row * ldda;
+  for (int64_t k = lane; k < K; k += 32) out[k] = 0.f;
+  __syncwarp();
+  const T* g = G + row * ldg;
+  BitWalker wk;
+  wk.init(A + row * Kw, 0, (int)Kw, lane);
+  for (uint32_t k = wk.next(); k != kEnd; k = wk.next()) {
+    const T* x = X + (int64_t)k * ldx;
+    float s = 0.f;
+    for (int64_t j = lane; j < N; j += 32) s = fmaf(to_f32(g[j]), to_f32(x[j]), s);
+#pragma unroll
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(kFull, s, o);
+    if (lane == 0) out[k] = s;
+  }
+}
+
 }  // namespace
+
+int launch_sddmm_rows(const uint32_t* A, int64_t M, int64_t K, const void* G, int64_t ldg, const void* X,
+                      int64_t ldx, int dt, int64_t N, float* dA, int64_t ldda, cudaStream_t s) {
+  if (M == 0 || K == 0) return BSP_OK;
+  const unsigned grid = (unsigned)ceil_div(M, 8);
+  const int64_t Kw = ceil_div(K, 32);
+  switch (dt) {
+    case BSP_F32: k_sddmm_rows<float><<<grid, 256, 0, s>>>(A, M, K, Kw, (const float*)G, ldg, (const float*)X, ldx, N, dA, ldda); break;
+    case BSP_BF16: k_sddmm_rows<__nv_bfloat16><<<grid, 256, 0, s>>>(A, M, K, Kw, (const __nv_bfloat16*)G, ldg, (const __nv_bfloat16*)X, ldx, N, dA, ldda); break;
+    case BSP_F16: k_sddmm_rows<__half><<<grid, 256, 0, s>>>(A, M, K, Kw, (const __half*)G, ldg, (const __half*)X, ldx, N, dA, ldda); break;
+    default: return BSP_ERR_UNSUPPORTED;
+  }
+  BSP_LAUNCHED();
+  return BSP_OK;
+}
 
 int launch_spmm_rows(const SpmmArgs& a, bool proto, bool vec, cudaStream_t s) {
   if (a.M == 0 || a.N == 0) return BSP_OK;

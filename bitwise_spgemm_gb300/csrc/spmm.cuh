@@ -44,9 +44,22 @@ int bulk_device_error(int* out, bool clear);
 // K tiles per 128-row block ([ceil(M/128)][tc_occupancy_words(K)]), then the
 // tcgen05 kernel over the occupied tiles.
 int tc_occupancy_words(int64_t K);
+int tc_occupancy_t_words(int64_t M);
 int launch_tile_occupancy(const uint32_t* A, int64_t M, int64_t K, uint32_t* occ,
                           unsigned long long* count, cudaStream_t s);
+// Occupancy of Aᵀ: [ceil(K/128)][tc_occupancy_t_words(M)], bit = 32-row tile
+int launch_tile_occupancy_t(const uint32_t* A, int64_t M, int64_t K, uint32_t* occT,
+                            unsigned long long* count, cudaStream_t s);
 int launch_spmm_tc(const SpmmArgs& a, const uint32_t* occ, cudaStream_t s);
+// dX[K][N] = Aᵀ·G on the tensor cores, Aᵀ read from A's row words
+int launch_spmm_t_tc(const uint32_t* A, int64_t M, int64_t K, const void* G, int gdt, int64_t ldg, int64_t N,
+                     float* dX, int64_t lddx, const uint32_t* occT, cudaStream_t s);
+// dA[M][K] = (G·Xᵀ) at A's set bits, 0 elsewhere, on the tensor cores
+int launch_sddmm_tc(const uint32_t* A, int64_t M, int64_t K, const void* G, int64_t ldg, const void* X,
+                    int64_t ldx, int dt, int64_t N, float* dA, int64_t ldda, cudaStream_t s);
+// same on CUDA cores (any dtype / layout): warp per row, one dot product per set bit
+int launch_sddmm_rows(const uint32_t* A, int64_t M, int64_t K, const void* G, int64_t ldg, const void* X,
+                      int64_t ldx, int dt, int64_t N, float* dA, int64_t ldda, cudaStream_t s);
 int tc_device_error(int* out, bool clear);
 
 

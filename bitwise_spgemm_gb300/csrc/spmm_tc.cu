@@ -44,15 +44,16 @@ constexpr int kTcThreads = 160;
 // costs one CTA per SM).
 constexpr bool kGuard = false;
 constexpr uint32_t kTmemCols = kGuard ? 512 : 256;
-// Operands are stored as 8x16-byte core matrices (no swizzle).  In both
-// descriptors the leading byte offset (LBO) is the distance between core
-// matrices adjacent along K and the stride byte offset (SBO) the distance
-// between core matrices adjacent along M (A) or N (B) — measured on GB300
+// Operands are stored as 8x16-byte core matrices (no swizzle).  In every
+// descriptor the leading byte offset (LBO) is the distance between core
+// matrices adjacent along the reduction (K) and the stride byte offset (SBO)
+// the distance between core matrices adjacent along M (operand A) or N
+// (operand B), for K-major and MN-major operands alike — measured on GB300
 // with one-hot A rows and position-encoding B values.
-// A (K-major):  element (m, k) at (m/8)*kASbo + (k/8)*kALbo + (m%8)*16 + (k%8)*2
-constexpr uint32_t kALbo = 128, kASbo = 512;
-// B (MN-major): element (k, n) at (n/8)*kBSbo + (k/8)*kBLbo + (k%8)*16 + (n%8)*2
-constexpr uint32_t kBLbo = 128, kBSbo = 512;
+//   K-major:  element (mn, k) at (mn/8)*kSbo + (k/8)*kLbo + (mn%8)*16 + (k%8)*2
+//   MN-major: element (k, mn) at (mn/8)*kSbo + (k/8)*kLbo + (k%8)*16 + (mn%8)*2
+constexpr uint32_t kLbo = 128, kSbo = 512;
+constexpr int kFwd = 0, kTrans = 1, kSddmm = 2;
 
 struct __align__(1024) TcSmem {
   uint8_t a[kStages][kAStage];
@@ -65,10 +66,11 @@ struct __align__(1024) TcSmem {
   uint8_t guard[kGuard ? 65536 : 16];
 };
 
-// Instruction descriptor for kind::f16: D f32, A and B of the same 16-bit
-// type (bf16 = 1, f16 = 0), A K-major, B MN-major, N = 256, M = 128.
-__host__ __device__ constexpr uint32_t idesc_f16(uint32_t ab_type) {
-  return (1u << 4) | (ab_type << 7) | (ab_type << 10) | (0u << 15) | (1u << 16) |
+// Instruction descriptor for kind::f16: D f32 (bits 4-5), A and B of the
+// same 16-bit type (bits 7-9, 10-12: bf16 = 1, f16 = 0), A / B major (bits
+// 15, 16: 0 = K-major, 1 = MN-major), N >> 3 (bits 17-22), M >> 4 (24-28).
+__host__ __device__ constexpr uint32_t idesc_f16(uint32_t ab_type, uint32_t a_mn, uint32_t b_mn) {
+  return (1u << 4) | (ab_type << 7) | (ab_type << 10) | (a_mn << 15) | (b_mn << 16) |
          ((uint32_t)(kTcN >> 3) << 17) | ((uint32_t)(kTcM >> 4) << 24);
 }
 
@@ -80,6 +82,21 @@ __device__ __forceinline__ uint4 expand8(uint32_t byte, uint32_t one) {
     w[j] = (((byte >> (2 * j)) & 1u) ? one : 0u) | ((((byte >> (2 * j + 1)) & 1u) ? one : 0u) << 16);
   return make_uint4(w[0], w[1], w[2], w[3]);
 }
+
+struct TcArgs {
+  const uint32_t* A;  // bit matrix, packed rows [M][Kw]
+  int64_t M, K, Kw;
+  const void* B;      // fwd: B [K][ldb]; trans: G [M][ldb]; sddmm: X [K][ldb]
+  int64_t ldb;
+  const void* G;      // sddmm: G [M][ldg]
+  int64_t ldg;
+  int64_t N;
+  float* C;           // fwd: C [M][ldc]; trans: dX [K][ldc]; sddmm: dA [M][ldc]
+  int64_t ldc;
+  const uint32_t* occ;  // fwd / trans occupancy bitmap (unused by sddmm)
+  int occ_words;
+  int bdt;
+};
 
 struct TileIter {  // set bits of the block's occupancy words, ascending
   const uint32_t* occ;
@@ -102,16 +119,44 @@ struct TileIter {  // set bits of the block's occupancy words, ascending
   }
 };
 
-template <typename BT>
-__global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(SpmmArgs a, const uint32_t* __restrict__ occ,
-                                                          int occ_words) {
+// Steps of the reduction: occupied tiles from a bitmap (forward: K tiles of
+// the CTA's 128-row block; transposed: row tiles of its 128-column block) or
+// every 32-column step of N (SDDMM).
+struct StepIter {
+  TileIter it;
+  int dense_left, dense_i;
+  bool dense;
+  __device__ void init(const uint32_t* occ, int words, int dense_steps, bool is_dense) {
+    dense = is_dense;
+    dense_left = dense_steps;
+    dense_i = 0;
+    if (!dense) it.init(occ, words);
+  }
+  __device__ __forceinline__ int next() {
+    if (dense) return dense_left-- > 0 ? dense_i++ : -1;
+    return it.next();
+  }
+};
+
+// One kernel, three products (MODE):
+//   kFwd   C[M,N]  = A · B        A bits K-major from A's words, B MN-major
+//   kTrans C[K,N]  = Aᵀ · G       Aᵀ MN-major built from A's row words (no
+//                                 transposed copy), G MN-major
+//   kSddmm dA[M,K] = (G · Xᵀ) ⊙ A  G and X K-major (16-byte cp.async),
+//                                 dense over N, masked store
+// All three use the same core-matrix geometry (LBO = 128 B along the
+// reduction, SBO = 512 B along M/N) and differ only in the producers, the
+// instruction descriptor's major bits and the epilogue.
+template <typename BT, int MODE>
+__global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   TcSmem& sm = *reinterpret_cast<TcSmem*>(smem_raw);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int64_t row0 = (int64_t)blockIdx.x * kTcM;
-  const int n0 = (int)blockIdx.y * kTcN;
+  const int64_t row0 = (int64_t)blockIdx.x * kTcM;  // output rows: M (fwd, sddmm) or K (trans)
+  const int64_t col0 = (int64_t)blockIdx.y * kTcN;  // output columns: N (fwd, trans) or K (sddmm)
+  const int64_t out_rows = MODE == kTrans ? a.K : a.M;
+  const int64_t out_cols = MODE == kSddmm ? a.K : a.N;
   const uint32_t one = std::is_same<BT, __nv_bfloat16>::value ? 0x3f80u : 0x3c00u;
-  const uint32_t* block_occ = occ + (int64_t)blockIdx.x * occ_words;
 
   if (tid == 0) {
     for (int s = 0; s < kStages; s++) {
@@ -126,21 +171,32 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(SpmmArgs a, const uin
     ptx::tmem_alloc(&sm.tmem_addr, kTmemCols);
     ptx::tmem_relinquish();
   }
+  // SDDMM: a block of A without set bits needs no product at all
+  int any = 1;
+  if (MODE == kSddmm) {
+    uint32_t acc = 0;
+    if (warp < 4 && row0 + tid < a.M) {
+      const uint32_t* arow = a.A + (row0 + tid) * a.Kw;
+      for (int64_t w = col0 / 32; w < min(a.Kw, (col0 + kTcN) / 32); w++) acc |= __ldg(arow + w);
+    }
+    any = __syncthreads_or(acc != 0u);
+  }
   ptx::tc_fence_before_sync();
   __syncthreads();
   ptx::tc_fence_after_sync();
   const uint32_t tmem = sm.tmem_addr;
+  const int dense_steps = any ? (int)((a.N + kTcK - 1) / kTcK) : 0;
+  const uint32_t* block_occ = a.occ + (int64_t)blockIdx.x * a.occ_words;
   int ntiles = 0;
 
   if (warp < 4) {
     // ---------------- producers ----------------
-    const BT* __restrict__ B = static_cast<const BT*>(a.B);
-    const int64_t arow = row0 + tid;
-    const uint32_t* awords = a.A + arow * a.Kw;
-    TileIter it;
-    it.init(block_occ, occ_words);
+    const BT* __restrict__ Bsrc = static_cast<const BT*>(a.B);
+    const BT* __restrict__ Gsrc = static_cast<const BT*>(a.G);
+    StepIter it;
+    it.init(block_occ, a.occ_words, dense_steps, MODE == kSddmm);
     int i = 0;
-    for (int kt = it.next(); kt >= 0; kt = it.next(), i++) {
+    for (int t = it.next(); t >= 0; t = it.next(), i++) {
       const int s = i % kStages;
       if (i >= kStages && !ptx::mbar_wait(&sm.empty[s], ((i / kStages) - 1) & 1)) {
         atomicCAS(&g_tc_error, 0, 3);
@@ -148,26 +204,65 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(SpmmArgs a, const uin
         break;
       }
       if (*(volatile int*)&sm.abort) break;
-      // A operand: row tid, 32 columns → 4 core-matrix rows of 8 values
-      const uint32_t w = arow < a.M ? __ldg(awords + kt) : 0u;
-      uint8_t* as = sm.a[s] + (tid >> 3) * kASbo + (tid & 7) * 16;
+      if (MODE == kFwd) {
+        // A: row tid's word t → 4 core-matrix rows (K-major)
+        const int64_t arow = row0 + tid;
+        const uint32_t w = arow < a.M ? __ldg(a.A + arow * a.Kw + t) : 0u;
+        uint8_t* as = sm.a[s] + (tid >> 3) * kSbo + (tid & 7) * 16;
 #pragma unroll
-      for (int c = 0; c < 4; c++)
-        *reinterpret_cast<uint4*>(as + c * kALbo) = expand8((w >> (8 * c)) & 0xffu, one);
-      // B tile rows k0..k0+31, columns n0..n0+255: 1024 chunks of 16 bytes
-      const int64_t k0 = (int64_t)kt * kTcK;
+        for (int c = 0; c < 4; c++) *reinterpret_cast<uint4*>(as + c * kLbo) = expand8((w >> (8 * c)) & 0xffu, one);
+      } else if (MODE == kTrans) {
+        // Aᵀ: row j of the 32-row tile, word wk of the 128-column block →
+        // 4 core-matrix rows of the MN-major operand
+        const int j = tid & 31, wk = tid >> 5;
+        const int64_t arow = (int64_t)t * kTcK + j;
+        const int64_t wcol = row0 / 32 + wk;
+        const uint32_t w = (arow < a.M && wcol < a.Kw) ? __ldg(a.A + arow * a.Kw + wcol) : 0u;
+        uint8_t* as = sm.a[s] + (j >> 3) * kLbo + (j & 7) * 16;
 #pragma unroll
-      for (int j = 0; j < 8; j++) {
-        const int q = tid + kProducers * j;
-        const int k = q >> 5, n8 = q & 31;
-        const int64_t krow = k0 + k;
-        const int ncol = n0 + n8 * 8;
-        const bool ok = krow < a.K && ncol < a.N;
-        const BT* src = ok ? B + krow * a.ldb + ncol : B;
-        ptx::cp_async_16(sm.b[s] + n8 * kBSbo + (k >> 3) * kBLbo + (k & 7) * 16, src, ok ? 16u : 0u);
+        for (int c = 0; c < 4; c++)
+          *reinterpret_cast<uint4*>(as + (wk * 4 + c) * kSbo) = expand8((w >> (8 * c)) & 0xffu, one);
+      } else {
+        // G tile: rows row0.., columns t*32.. (K-major), 512 chunks
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const int q = tid + kProducers * j;
+          const int m = q >> 2, k8 = q & 3;
+          const int64_t r = row0 + m;
+          const int64_t c = (int64_t)t * kTcK + k8 * 8;
+          const bool ok = r < a.M && c < a.N;
+          ptx::cp_async_16(sm.a[s] + (m >> 3) * kSbo + k8 * kLbo + (m & 7) * 16,
+                           ok ? Gsrc + r * a.ldg + c : Gsrc, ok ? 16u : 0u);
+        }
+      }
+      if (MODE == kSddmm) {
+        // X tile: rows col0.. (columns of dA), columns t*32.. (K-major), 1024 chunks
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          const int q = tid + kProducers * j;
+          const int nn = q >> 2, k8 = q & 3;
+          const int64_t r = col0 + nn;
+          const int64_t c = (int64_t)t * kTcK + k8 * 8;
+          const bool ok = r < a.K && c < a.N;
+          ptx::cp_async_16(sm.b[s] + (nn >> 3) * kSbo + k8 * kLbo + (nn & 7) * 16,
+                           ok ? Bsrc + r * a.ldb + c : Bsrc, ok ? 16u : 0u);
+        }
+      } else {
+        // B (fwd) / G (trans) tile: reduction rows t*32.., columns col0.. (MN-major)
+        const int64_t red_limit = MODE == kFwd ? a.K : a.M;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          const int q = tid + kProducers * j;
+          const int k = q >> 5, n8 = q & 31;
+          const int64_t krow = (int64_t)t * kTcK + k;
+          const int64_t ncol = col0 + n8 * 8;
+          const bool ok = krow < red_limit && ncol < a.N;
+          ptx::cp_async_16(sm.b[s] + n8 * kSbo + (k >> 3) * kLbo + (k & 7) * 16,
+                           ok ? Bsrc + krow * a.ldb + ncol : Bsrc, ok ? 16u : 0u);
+        }
       }
       ptx::cp_async_commit();
-      // stage i-2 is now complete: publish it to the MMA issuer
+      // step i-2 is now complete: publish it to the MMA issuer
       ptx::cp_async_wait_group<2>();
       if (i >= 2) {
         ptx::fence_proxy_async_smem();
@@ -180,11 +275,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(SpmmArgs a, const uin
     for (int j = (ntiles >= 2 ? ntiles - 2 : 0); j < ntiles; j++) ptx::mbar_arrive(&sm.full[j % kStages]);
   } else if (lane == 0) {
     // ---------------- MMA issuer ----------------
-    const uint32_t idesc = idesc_f16(std::is_same<BT, __nv_bfloat16>::value ? 1u : 0u);
-    TileIter it;
-    it.init(block_occ, occ_words);
+    const uint32_t ab = std::is_same<BT, __nv_bfloat16>::value ? 1u : 0u;
+    const uint32_t idesc = idesc_f16(ab, MODE == kTrans ? 1u : 0u, MODE == kSddmm ? 0u : 1u);
+    StepIter it;
+    it.init(block_occ, a.occ_words, dense_steps, MODE == kSddmm);
     int i = 0;
-    for (int kt = it.next(); kt >= 0; kt = it.next(), i++) {
+    for (int t = it.next(); t >= 0; t = it.next(), i++) {
       const int s = i % kStages;
       if (!ptx::mbar_wait(&sm.full[s], (i / kStages) & 1)) {
         atomicCAS(&g_tc_error, 0, 3);
@@ -195,8 +291,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(SpmmArgs a, const uin
       ptx::tc_fence_after_sync();
 #pragma unroll
       for (int j = 0; j < 2; j++) {
-        const uint64_t ad = ptx::smem_desc_noswizzle(sm.a[s] + j * 2 * kALbo, kALbo, kASbo);
-        const uint64_t bd = ptx::smem_desc_noswizzle(sm.b[s] + j * 2 * kBLbo, kBLbo, kBSbo);
+        const uint64_t ad = ptx::smem_desc_noswizzle(sm.a[s] + j * 2 * kLbo, kLbo, kSbo);
+        const uint64_t bd = ptx::smem_desc_noswizzle(sm.b[s] + j * 2 * kLbo, kLbo, kSbo);
         ptx::tc_mma_f16(tmem, ad, bd, idesc, (i > 0) || (j > 0));
       }
       ptx::tc_commit(&sm.empty[s]);
@@ -215,8 +311,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(SpmmArgs a, const uin
     }
     ptx::tc_fence_after_sync();
     const int64_t row = row0 + warp * 32 + lane;
-    float* crow = a.C + row * a.ldc + n0;
-    const bool live = row < a.M && ok && !*(volatile int*)&sm.abort;
+    float* crow = a.C + row * a.ldc + col0;
+    const bool live = row < out_rows && ok && !*(volatile int*)&sm.abort;
+    const uint32_t* arow = a.A + row * a.Kw;
     for (int c8 = 0; c8 < kTcN / 8; c8 += 4) {
       uint32_t r[4][8];
       if (have && ok) {
@@ -230,19 +327,21 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(SpmmArgs a, const uin
 #pragma unroll
           for (int q = 0; q < 8; q++) r[u][q] = 0u;
       }
-      if (live) {
+      if (!live) continue;
 #pragma unroll
-        for (int u = 0; u < 4; u++) {
-          const int col = (c8 + u) * 8;
-          if (n0 + col < a.N) {
-            *reinterpret_cast<float4*>(crow + col) =
-                make_float4(__uint_as_float(r[u][0]), __uint_as_float(r[u][1]), __uint_as_float(r[u][2]),
-                            __uint_as_float(r[u][3]));
-            *reinterpret_cast<float4*>(crow + col + 4) =
-                make_float4(__uint_as_float(r[u][4]), __uint_as_float(r[u][5]), __uint_as_float(r[u][6]),
-                            __uint_as_float(r[u][7]));
-          }
+      for (int u = 0; u < 4; u++) {
+        const int col = (c8 + u) * 8;
+        if (col0 + col >= out_cols) continue;
+        if (MODE == kSddmm) {  // keep the set bits of A's row only
+          const uint32_t bits = (__ldg(arow + (col0 + col) / 32) >> ((col0 + col) & 31)) & 0xffu;
+#pragma unroll
+          for (int q = 0; q < 8; q++)
+            if (!((bits >> q) & 1u)) r[u][q] = 0u;
         }
+        *reinterpret_cast<float4*>(crow + col) = make_float4(
+            __uint_as_float(r[u][0]), __uint_as_float(r[u][1]), __uint_as_float(r[u][2]), __uint_as_float(r[u][3]));
+        *reinterpret_cast<float4*>(crow + col + 4) = make_float4(
+            __uint_as_float(r[u][4]), __uint_as_float(r[u][5]), __uint_as_float(r[u][6]), __uint_as_float(r[u][7]));
       }
     }
   }
@@ -251,6 +350,28 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(SpmmArgs a, const uin
   if (warp == 4) {
     ptx::tc_fence_after_sync();
     ptx::tmem_dealloc(tmem, kTmemCols);
+  }
+}
+
+// Occupancy of Aᵀ's tiles: warp per (128-column block of A, 32 consecutive
+// 32-row tiles); lane = row tile, OR of 32 rows x 4 words, one ballot.
+__global__ void __launch_bounds__(256) k_tile_occupancy_t(const uint32_t* __restrict__ A, int64_t M, int64_t Kw,
+                                                          int occ_words, int64_t nkb, uint32_t* __restrict__ occ,
+                                                          unsigned long long* __restrict__ count) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  if (warp >= nkb * occ_words) return;
+  const int64_t kb = warp / occ_words;
+  const int ow = (int)(warp - kb * occ_words);
+  const int64_t it = (int64_t)ow * 32 + lane;
+  uint32_t acc = 0;
+  const int64_t r0 = it * kTcK, r1 = min(M, r0 + kTcK);
+  for (int64_t r = r0; r < r1; r++)
+    for (int64_t w = kb * 4; w < min(Kw, kb * 4 + 4); w++) acc |= __ldg(A + r * Kw + w);
+  const uint32_t m = __ballot_sync(kFull, acc != 0u);
+  if (lane == 0) {
+    occ[warp] = m;
+    if (count && m) atomicAdd(count, (unsigned long long)__popc(m));
   }
 }
 
@@ -281,6 +402,7 @@ __global__ void __launch_bounds__(256) k_tile_occupancy(const uint32_t* __restri
 }  // namespace
 
 int tc_occupancy_words(int64_t K) { return (int)ceil_div(ceil_div(K, 32), 32); }
+int tc_occupancy_t_words(int64_t M) { return (int)ceil_div(ceil_div(M, 32), 32); }
 
 int launch_tile_occupancy(const uint32_t* A, int64_t M, int64_t K, uint32_t* occ,
                           unsigned long long* count, cudaStream_t s) {
@@ -292,27 +414,97 @@ int launch_tile_occupancy(const uint32_t* A, int64_t M, int64_t K, uint32_t* occ
   return BSP_OK;
 }
 
-int launch_spmm_tc(const SpmmArgs& a, const uint32_t* occ, cudaStream_t s) {
-  if (a.M == 0 || a.N == 0) return BSP_OK;
-  const size_t smem = sizeof(TcSmem);
-  const dim3 grid((unsigned)ceil_div(a.M, kTcM), (unsigned)ceil_div(a.N, kTcN));
-  if (grid.y > 65535) return BSP_ERR_CAPACITY;
-  int dev = 0;
-  BSP_CUDA(cudaGetDevice(&dev));
-  static bool configured[2][64] = {};
-  const int t = a.bdt == BSP_BF16 ? 0 : 1;
-  if (dev < 64 && !configured[t][dev]) {
-    if (t == 0)
-      BSP_CUDA(cudaFuncSetAttribute(k_spmm_tc<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    else
-      BSP_CUDA(cudaFuncSetAttribute(k_spmm_tc<__half>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    configured[t][dev] = true;
-  }
-  const int ow = tc_occupancy_words(a.K);
-  if (t == 0) k_spmm_tc<__nv_bfloat16><<<grid, kTcThreads, smem, s>>>(a, occ, ow);
-  else k_spmm_tc<__half><<<grid, kTcThreads, smem, s>>>(a, occ, ow);
+int launch_tile_occupancy_t(const uint32_t* A, int64_t M, int64_t K, uint32_t* occT,
+                            unsigned long long* count, cudaStream_t s) {
+  const int ow = tc_occupancy_t_words(M);
+  const int64_t nkb = ceil_div(K, kTcM);
+  const int64_t warps = nkb * ow;
+  if (warps == 0) return BSP_OK;
+  k_tile_occupancy_t<<<(unsigned)ceil_div(warps, 8), 256, 0, s>>>(A, M, ceil_div(K, 32), ow, nkb, occT, count);
   BSP_LAUNCHED();
   return BSP_OK;
+}
+
+namespace {
+template <typename BT, int MODE>
+int launch_mode(const TcArgs& a, dim3 grid, cudaStream_t s) {
+  const size_t smem = sizeof(TcSmem);
+  static bool configured[64] = {};
+  int dev = 0;
+  BSP_CUDA(cudaGetDevice(&dev));
+  if (dev < 64 && !configured[dev]) {
+    BSP_CUDA(cudaFuncSetAttribute(k_spmm_tc<BT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    configured[dev] = true;
+  }
+  k_spmm_tc<BT, MODE><<<grid, kTcThreads, smem, s>>>(a);
+  BSP_LAUNCHED();
+  return BSP_OK;
+}
+
+template <int MODE>
+int launch_tc(const TcArgs& a, cudaStream_t s) {
+  const int64_t rows = MODE == kTrans ? a.K : a.M;
+  const int64_t cols = MODE == kSddmm ? a.K : a.N;
+  if (rows == 0 || cols == 0) return BSP_OK;
+  const dim3 grid((unsigned)ceil_div(rows, kTcM), (unsigned)ceil_div(cols, kTcN));
+  if (ceil_div(cols, kTcN) > 65535 || ceil_div(rows, kTcM) > 0x7fffffff) return BSP_ERR_CAPACITY;
+  if (a.bdt == BSP_BF16) return launch_mode<__nv_bfloat16, MODE>(a, grid, s);
+  if (a.bdt == BSP_F16) return launch_mode<__half, MODE>(a, grid, s);
+  return BSP_ERR_UNSUPPORTED;
+}
+}  // namespace
+
+int launch_spmm_tc(const SpmmArgs& sa, const uint32_t* occ, cudaStream_t s) {
+  TcArgs a = {};
+  a.A = sa.A;
+  a.M = sa.M;
+  a.K = sa.K;
+  a.Kw = sa.Kw;
+  a.B = sa.B;
+  a.ldb = sa.ldb;
+  a.N = sa.N;
+  a.C = sa.C;
+  a.ldc = sa.ldc;
+  a.occ = occ;
+  a.occ_words = tc_occupancy_words(sa.K);
+  a.bdt = sa.bdt;
+  return launch_tc<kFwd>(a, s);
+}
+
+int launch_spmm_t_tc(const uint32_t* A, int64_t M, int64_t K, const void* G, int gdt, int64_t ldg, int64_t N,
+                     float* dX, int64_t lddx, const uint32_t* occT, cudaStream_t s) {
+  TcArgs a = {};
+  a.A = A;
+  a.M = M;
+  a.K = K;
+  a.Kw = ceil_div(K, 32);
+  a.B = G;
+  a.ldb = ldg;
+  a.N = N;
+  a.C = dX;
+  a.ldc = lddx;
+  a.occ = occT;
+  a.occ_words = tc_occupancy_t_words(M);
+  a.bdt = gdt;
+  return launch_tc<kTrans>(a, s);
+}
+
+int launch_sddmm_tc(const uint32_t* A, int64_t M, int64_t K, const void* G, int64_t ldg, const void* X,
+                    int64_t ldx, int dt, int64_t N, float* dA, int64_t ldda, cudaStream_t s) {
+  TcArgs a = {};
+  a.A = A;
+  a.M = M;
+  a.K = K;
+  a.Kw = ceil_div(K, 32);
+  a.B = X;
+  a.ldb = ldx;
+  a.G = G;
+  a.ldg = ldg;
+  a.N = N;
+  a.C = dA;
+  a.ldc = ldda;
+  a.bdt = dt;
+  return launch_tc<kSddmm>(a, s);
 }
 
 int tc_device_error(int* out, bool clear) {

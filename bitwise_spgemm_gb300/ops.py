@@ -172,3 +172,34 @@ def spmm(words, K, B, plan=None, out=None, workspace=None):
     call("bsp_spmm", _p(words), M, K, _p(B), _DT[B.dtype], ldb, N, _p(out), ldc, h, ws_ptr, ws_n,
          _stream())
     return out
+
+
+def spmm_t(words, M, K, G, plan=None, out=None, workspace=None):
+    """dX = Aᵀ·G (FP32 [K, N]).  A: packed rows [M, ceil(K/32)], G: [M, N]."""
+    ldg = _rowmajor(G, "G")
+    N = G.shape[1]
+    if out is None:
+        out = torch.empty((K, N), dtype=torch.float32, device=G.device)
+    n = C.c_size_t()
+    call("bsp_spmm_t_workspace", M, K, C.byref(n))
+    if workspace is None or workspace.numel() * workspace.element_size() < n.value:
+        workspace = torch.empty(n.value, dtype=torch.uint8, device=G.device)
+    call("bsp_spmm_t", _p(words), M, K, _p(G), _DT[G.dtype], ldg, N, _p(out), out.stride(0),
+         plan.handle if plan is not None else None, _p(workspace),
+         workspace.numel() * workspace.element_size(), _stream())
+    return out
+
+
+def sddmm(words, M, K, G, X, plan=None, out=None):
+    """Straight-through mask gradient: dense [M, K] FP32 with (G·Xᵀ)[i, k] at
+    A's set bits and 0 elsewhere.  G: [M, N], X: [K, N], same dtype."""
+    ldg = _rowmajor(G, "G")
+    ldx = _rowmajor(X, "X")
+    if G.dtype != X.dtype:
+        raise ValueError("G and X must have the same dtype")
+    N = G.shape[1]
+    if out is None:
+        out = torch.empty((M, K), dtype=torch.float32, device=G.device)
+    call("bsp_sddmm", _p(words), M, K, _p(G), ldg, _p(X), ldx, _DT[G.dtype], N, _p(out),
+         out.stride(0), plan.handle if plan is not None else None, _stream())
+    return out

@@ -214,6 +214,34 @@ int bsp_spmm(const uint32_t* A_words, int64_t M, int64_t K, const void* B,
              const bsp_plan* plan, void* workspace, size_t workspace_bytes,
              bsp_stream_t stream);
 
+/* ======================================================================== */
+/* Backward pass                                                            */
+/* ======================================================================== */
+
+/* dX[K×N] (FP32, row stride lddx) = Aᵀ·G for G[M×N] of g_dtype (row stride
+ * ldg).  With a plan and 16-bit G the tensor cores read Aᵀ's bit tiles
+ * straight from A's row words (no transposed copy is made); otherwise the
+ * bits are transposed into the workspace (bsp_spmm_t_workspace bytes) and
+ * walked like bsp_spmm.  The backward of the forward SpMM; no reference
+ * counterpart (the reference has no backward).                            */
+int bsp_spmm_t_workspace(int64_t M, int64_t K, size_t* bytes);
+int bsp_spmm_t(const uint32_t* A_words, int64_t M, int64_t K, const void* G,
+               int g_dtype, int64_t ldg, int64_t N, float* dX, int64_t lddx,
+               const bsp_plan* plan, void* workspace, size_t workspace_bytes,
+               bsp_stream_t stream);
+
+/* Straight-through mask gradient: dA[M×K] (FP32, row stride ldda) =
+ * Σ_j G[i][j]·X[k][j] where A has bit (i,k) set, 0 elsewhere — the SDDMM of
+ * G[M×N] and X[K×N] (same dtype).  16-bit operands run on the tensor cores
+ * (dense product over N, masked store; blocks of A without bits skipped);
+ * FP32 or unaligned operands use one warp dot product per set bit.  The
+ * plan (optional) feeds the choice between the two.  No reference
+ * counterpart.                                                            */
+int bsp_sddmm(const uint32_t* A_words, int64_t M, int64_t K, const void* G,
+              int64_t ldg, const void* X, int64_t ldx, int dtype, int64_t N,
+              float* dA, int64_t ldda, const bsp_plan* plan,
+              bsp_stream_t stream);
+
 /* bsp_spmm without a workspace argument, for callers that may not allocate
  * device memory when they run the SpMM (plugin callbacks handed only
  * pointers, code inside CUDA stream capture, processes whose device memory
