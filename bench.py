@@ -43,9 +43,11 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=10)
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--config", default="c2", choices=["c1", "c2", "c3"],
+    p.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
                    help="c2 (default): clustered FP32 8192x8192x512; c1: 1024x1024x256 "
-                        "integer B; c3: block-structured 16384x16384x2048 BF16 (tensor cores)")
+                        "integer B; c3: block-structured 16384x16384x2048 BF16 (tensor cores); "
+                        "c4: 512 batched problems, N=128 BF16; "
+                        "c5: forward+backward of a 4096x4096 mask with 4096x8192 BF16 X")
     return p.parse_args()
 
 
@@ -445,10 +447,172 @@ def run_other(args):
     plan.close()
 
 
+def run_batched(args):
+    """Batched form: 512 independent problems (M, K log-uniform in [64, 4096],
+    density U(0.01, 0.3), N = 128, BF16 B) in one persistent graph-captured
+    launch, against looping the plain FP32 single-problem SpMM (also
+    graph-captured, so host launch overhead counts for neither)."""
+    import torch
+    from bitwise_spgemm_gb300 import capi, ops
+    from bitwise_spgemm_gb300 import workloads as W
+    ws, rank, local = dist_setup(args)
+    dev = torch.device("cuda", local)
+    probs = W.config4()
+    N = 128
+    items, items32 = [], []
+    comp = 0
+    nnz = 0
+    for pr in probs:
+        M, K = pr["M"], pr["K"]
+        wd = torch.from_numpy(np.ascontiguousarray(pr["words"]).view(np.int32)).to(dev)
+        B = torch.from_numpy(pr["B"].view(np.int16)).to(dev).view(torch.bfloat16)
+        items.append((wd, K, B, torch.empty(M, N, device=dev)))
+        items32.append((wd, K, B.float(), torch.empty(M, N, device=dev)))
+        comp += M * ((K + 31) // 32) * 4 + K * N * 2 + M * N * 4
+        nnz += int(np.unpackbits(np.ascontiguousarray(pr["words"]).view(np.uint8)).sum())
+    batch = ops.Batch(items)
+
+    def graph_of(fn):
+        fn()
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        st = torch.cuda.Stream(device=dev)
+        st.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(st):
+            with torch.cuda.graph(g, stream=st):
+                fn()
+        torch.cuda.synchronize()
+        return g
+
+    def loop32():
+        for wd, K, B32, Cd in items32:
+            ops.spmm(wd, K, B32, out=Cd)
+
+    gb = graph_of(batch.run)
+    g32 = graph_of(loop32)
+
+    def timed(g, steps, warm):
+        for _ in range(warm):
+            g.replay()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        cur = torch.cuda.current_stream()
+        e0.record(cur)
+        for _ in range(steps):
+            g.replay()
+        e1.record(cur)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    sampler = ClockSampler(local) if rank == 0 else None
+    if sampler:
+        sampler.start()
+    barrier(ws)
+    ms = max_over_ranks(ws, timed(gb, args.steps, max(args.warmup, 3)))
+    barrier(ws)
+    clocks = sampler.stop() if sampler else None
+    ms32 = timed(g32, 3, 1)
+    # spot check one problem against the FP32 loop
+    err = max(float((a[3] - b[3]).abs().max()) / max(float(b[3].abs().max()), 1e-30)
+              for a, b in zip(items[:8], items32[:8]))
+    out = {"metric": "batched bitmap-SpMM problems/s", "value": ws * len(probs) / (ms * 1e-3),
+           "unit": "problems/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "bf16", "data": "synthetic (seeded numpy, seed 7+i per problem)",
+           "config": {"workload": "batched_512_N128_bf16", "problems": len(probs), "N": N,
+                      "nnz": nnz, "graph": "one persistent launch, graph-captured"},
+           "aggregate_gbs": ws * comp / (ms * 1e-3) / 1e9,
+           "effective_tflops": 2.0 * nnz * N / (ms * 1e-3) / 1e12,
+           "fp32_loop_ms": ms32, "speedup_vs_fp32_loop": ms32 / ms,
+           "max_rel_diff_vs_fp32_loop": err, "clocks": clocks}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    batch.close()
+
+
+def run_fwd_bwd(args):
+    """Differentiable form: Y = A·X, dX = Aᵀ·G, dA = (G·Xᵀ) ⊙ A with A a
+    4096x4096 Bernoulli(0.1) mask, X and G 4096x8192 BF16; the same three
+    products in the plain FP32 form (CUDA cores) are timed for the speedup."""
+    import torch
+    from bitwise_spgemm_gb300 import capi, ops
+    from bitwise_spgemm_gb300 import workloads as W
+    ws, rank, local = dist_setup(args)
+    dev = torch.device("cuda", local)
+    cfg = W.config5()
+    M, K, N = cfg["M"], cfg["K"], cfg["N"]
+    words = torch.from_numpy(np.ascontiguousarray(cfg["words"]).view(np.int32)).to(dev)
+    X = torch.from_numpy(cfg["X"].view(np.int16)).to(dev).view(torch.bfloat16)
+    G = torch.from_numpy(cfg["G"].view(np.int16)).to(dev).view(torch.bfloat16)
+    plan = ops.Plan(words, K)
+    info = plan.info()
+    Y = torch.empty(M, N, device=dev)
+    dX = torch.empty(K, N, device=dev)
+    dA = torch.empty(M, K, device=dev)
+    wsp = torch.empty(max(plan.workspace_bytes(N), 16), dtype=torch.uint8, device=dev)
+
+    def step16():
+        ops.spmm(words, K, X, plan=plan, out=Y, workspace=wsp)
+        ops.spmm_t(words, M, K, G, plan=plan, out=dX)
+        ops.sddmm(words, M, K, G, X, plan=plan, out=dA)
+
+    X32, G32 = X.float(), G.float()
+
+    def step32():
+        ops.spmm(words, K, X32, plan=plan, out=Y, workspace=wsp)
+        ops.spmm_t(words, M, K, G32, plan=plan, out=dX)
+        ops.sddmm(words, M, K, G32, X32, plan=plan, out=dA)
+
+    def timed(fn, steps, warm):
+        for _ in range(warm):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        cur = torch.cuda.current_stream()
+        e0.record(cur)
+        for _ in range(steps):
+            fn()
+        e1.record(cur)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    sampler = ClockSampler(local) if rank == 0 else None
+    if sampler:
+        sampler.start()
+    barrier(ws)
+    ms = max_over_ranks(ws, timed(step16, args.steps, max(args.warmup, 3)))
+    barrier(ws)
+    clocks = sampler.stop() if sampler else None
+    ms32 = timed(step32, 2, 1)
+    nnz = info["nnz"]
+    useful = 3 * 2.0 * nnz * N
+    dense = 3 * 2.0 * M * K * N
+    tp, tkind = tensor_peak()
+    comp = 2 * (M * ((K + 31) // 32) * 4) + 2 * K * N * 2 + 2 * M * N * 2 + M * N * 4 + K * N * 4 + M * K * 4
+    out = {"metric": "bitmap-SpMM forward+backward ms (Y, dX, dA)", "value": ms, "unit": "ms",
+           "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+           "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
+           "data": "synthetic (seeded numpy)",
+           "config": {"workload": "mask_4096x4096_x_4096x8192_fwd_bwd_bf16", "M": M, "K": K, "N": N,
+                      "nnz": nnz},
+           "fp32_form_ms": ms32, "speedup_vs_fp32_form": ms32 / ms,
+           "effective_tflops": useful / (ms * 1e-3) / 1e12,
+           "tensor": {"dense_tflops": dense / (ms * 1e-3) / 1e12, "peak_tflops": tp,
+                      "frac": dense / (ms * 1e-3) / 1e12 / tp, "peak_source": tkind},
+           "gbs_compulsory": comp / (ms * 1e-3) / 1e9, "clocks": clocks}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    plan.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.config == "c5":
+        run_fwd_bwd(args)
+    elif args.config == "c4":
+        run_batched(args)
     elif args.config != "c2":
         run_other(args)
     else:

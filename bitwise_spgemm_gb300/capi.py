@@ -40,6 +40,11 @@ class PlanInfo(C.Structure):
                 ("direct_rows", C.c_int64), ("direct_nnz", C.c_int64), ("occ_tiles", C.c_int64)]
 
 
+class Problem(C.Structure):
+    _fields_ = [("A_words", C.c_void_p), ("M", C.c_int64), ("K", C.c_int64), ("B", C.c_void_p),
+                ("ldb", C.c_int64), ("C", C.c_void_p), ("ldc", C.c_int64)]
+
+
 _P = C.c_void_p
 _I64 = C.c_int64
 _I = C.c_int
@@ -64,6 +69,9 @@ SIGNATURES = {
     "bsp_spmm": [_P, _I64, _I64, _P, _I, _I64, _I64, _P, _I64, _P, _P, _SZ, _P],
     "bsp_device_status": [C.POINTER(_I), _I],
     "bsp_spmm_t_workspace": [_I64, _I64, C.POINTER(_SZ)],
+    "bsp_batch_create": [C.POINTER(Problem), _I, _I64, _I, C.POINTER(_P), _P],
+    "bsp_batch_destroy": [_P],
+    "bsp_batched_spmm": [_P, _P],
     "bsp_spmm_t": [_P, _I64, _I64, _P, _I, _I64, _I64, _P, _I64, _P, _P, _SZ, _P],
     "bsp_sddmm": [_P, _I64, _I64, _P, _I64, _P, _I64, _I, _I64, _P, _I64, _P, _P],
     "bsp_spmm_noalloc": [_P, _I64, _I64, _P, _I, _I64, _I64, _P, _I64, _P, _P],

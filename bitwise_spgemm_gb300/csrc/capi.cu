@@ -414,10 +414,11 @@ int bsp_sddmm(const uint32_t* A_words, int64_t M, int64_t K, const void* G, int6
 
 int bsp_device_status(int* status, int clear) {
   if (!status) return BSP_ERR_INVALID_ARG;
-  int a = 0, b = 0;
+  int a = 0, b = 0, c = 0;
   BSP_TRY(bulk_device_error(&a, clear != 0));
   BSP_TRY(tc_device_error(&b, clear != 0));
-  *status = a ? a : b;
+  BSP_TRY(batched_device_error(&c, clear != 0));
+  *status = a ? a : (b ? b : c);
   return BSP_OK;
 }
 

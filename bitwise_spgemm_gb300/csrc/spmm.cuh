@@ -61,6 +61,7 @@ int launch_sddmm_tc(const uint32_t* A, int64_t M, int64_t K, const void* G, int6
 int launch_sddmm_rows(const uint32_t* A, int64_t M, int64_t K, const void* G, int64_t ldg, const void* X,
                       int64_t ldx, int dt, int64_t N, float* dA, int64_t ldda, cudaStream_t s);
 int tc_device_error(int* out, bool clear);
+int batched_device_error(int* out, bool clear);
 
 
 

@@ -23,6 +23,7 @@
 
 #include "ptx.cuh"
 #include "spmm_dev.cuh"
+#include "tc_common.cuh"
 
 namespace bsp {
 
@@ -44,15 +45,9 @@ constexpr int kTcThreads = 160;
 // costs one CTA per SM).
 constexpr bool kGuard = false;
 constexpr uint32_t kTmemCols = kGuard ? 512 : 256;
-// Operands are stored as 8x16-byte core matrices (no swizzle).  In every
-// descriptor the leading byte offset (LBO) is the distance between core
-// matrices adjacent along the reduction (K) and the stride byte offset (SBO)
-// the distance between core matrices adjacent along M (operand A) or N
-// (operand B), for K-major and MN-major operands alike — measured on GB300
-// with one-hot A rows and position-encoding B values.
-//   K-major:  element (mn, k) at (mn/8)*kSbo + (k/8)*kLbo + (mn%8)*16 + (k%8)*2
-//   MN-major: element (k, mn) at (mn/8)*kSbo + (k/8)*kLbo + (k%8)*16 + (mn%8)*2
-constexpr uint32_t kLbo = 128, kSbo = 512;
+using tc::kLbo;
+using tc::kSbo;
+using tc::expand8;
 constexpr int kFwd = 0, kTrans = 1, kSddmm = 2;
 
 struct __align__(1024) TcSmem {
@@ -66,21 +61,8 @@ struct __align__(1024) TcSmem {
   uint8_t guard[kGuard ? 65536 : 16];
 };
 
-// Instruction descriptor for kind::f16: D f32 (bits 4-5), A and B of the
-// same 16-bit type (bits 7-9, 10-12: bf16 = 1, f16 = 0), A / B major (bits
-// 15, 16: 0 = K-major, 1 = MN-major), N >> 3 (bits 17-22), M >> 4 (24-28).
 __host__ __device__ constexpr uint32_t idesc_f16(uint32_t ab_type, uint32_t a_mn, uint32_t b_mn) {
-  return (1u << 4) | (ab_type << 7) | (ab_type << 10) | (a_mn << 15) | (b_mn << 16) |
-         ((uint32_t)(kTcN >> 3) << 17) | ((uint32_t)(kTcM >> 4) << 24);
-}
-
-// 8 bits of a word → 8 16-bit values 0 / one, packed little-endian.
-__device__ __forceinline__ uint4 expand8(uint32_t byte, uint32_t one) {
-  uint32_t w[4];
-#pragma unroll
-  for (int j = 0; j < 4; j++)
-    w[j] = (((byte >> (2 * j)) & 1u) ? one : 0u) | ((((byte >> (2 * j + 1)) & 1u) ? one : 0u) << 16);
-  return make_uint4(w[0], w[1], w[2], w[3]);
+  return tc::idesc_f16(ab_type, a_mn, b_mn, kTcN, kTcM);
 }
 
 struct TcArgs {

@@ -203,3 +203,40 @@ def sddmm(words, M, K, G, X, plan=None, out=None):
     call("bsp_sddmm", _p(words), M, K, _p(G), ldg, _p(X), ldx, _DT[G.dtype], N, _p(out),
          out.stride(0), plan.handle if plan is not None else None, _stream())
     return out
+
+
+class Batch:
+    """Many independent C_i = A_i·B_i (16-bit B, shared N) in one persistent
+    tensor-core launch.  ``problems``: list of (words, K, B, C) tensors; the
+    tensors are referenced by the batch and must outlive it."""
+
+    def __init__(self, problems):
+        n = len(problems)
+        if n == 0:
+            raise ValueError("empty batch")
+        N = problems[0][2].shape[1]
+        dt = problems[0][2].dtype
+        arr = (capi.Problem * n)()
+        self._keep = []
+        for i, (words, K, B, Cout) in enumerate(problems):
+            if B.dtype != dt or B.shape[1] != N or Cout.shape[1] != N:
+                raise ValueError("all problems of a batch share N and the B dtype")
+            arr[i] = capi.Problem(words.data_ptr() if words.numel() else 0, words.shape[0], K,
+                                  B.data_ptr() if B.numel() else 0, _rowmajor(B, "B"),
+                                  Cout.data_ptr() if Cout.numel() else 0, _rowmajor(Cout, "C"))
+            self._keep.append((words, B, Cout))
+        h = C.c_void_p()
+        call("bsp_batch_create", arr, n, N, _DT[dt], C.byref(h), _stream())
+        self._h = h
+        self._lib = capi.lib()
+
+    def run(self):
+        call("bsp_batched_spmm", self._h, _stream())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.bsp_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()

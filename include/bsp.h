@@ -215,6 +215,37 @@ int bsp_spmm(const uint32_t* A_words, int64_t M, int64_t K, const void* B,
              bsp_stream_t stream);
 
 /* ======================================================================== */
+/* Batched SpMM                                                             */
+/* ======================================================================== */
+
+/* One problem of a batch: C[M×N] = A·B with A packed (LSB-first) words
+ * [M][ceil(K/32)] and B K×N (row stride ldb elements, 16-byte aligned,
+ * ldb*2 a multiple of 16), C FP32 (16-byte aligned, ldc a multiple of 4).  */
+typedef struct bsp_problem {
+  const uint32_t* A_words;
+  int64_t M, K;
+  const void* B;
+  int64_t ldb;
+  float* C;
+  int64_t ldc;
+} bsp_problem;
+
+typedef struct bsp_batch bsp_batch;
+
+/* Prepare a batch of n independent problems sharing N (multiple of 8) and a
+ * 16-bit B type: uploads the descriptors and a device work queue of
+ * (problem, 128-row block, column block) items sorted longest first;
+ * synchronises the stream once.  The problems' buffers are referenced, not
+ * copied — they must outlive the batch.  No reference counterpart (the
+ * reference runs one fixed-size problem per launch).                       */
+int bsp_batch_create(const bsp_problem* problems, int n, int64_t N,
+                     int b_dtype, bsp_batch** batch, bsp_stream_t stream);
+int bsp_batch_destroy(bsp_batch* batch);
+/* Every problem of the batch in one persistent tensor-core launch (no host
+ * synchronisation, no allocation: can be captured in a CUDA graph).       */
+int bsp_batched_spmm(const bsp_batch* batch, bsp_stream_t stream);
+
+/* ======================================================================== */
 /* Backward pass                                                            */
 /* ======================================================================== */
 

@@ -1,0 +1,94 @@
+"""Batched persistent tensor-core SpMM against the oracle: problems of uneven
+M, K and density, column blocking, empty problems and CUDA-graph replay.
+Scaled error against FP64 ≤ 1e-4 (BF16 products are exact, FP32
+accumulation), integer-valued B exact."""
+import numpy as np
+import pytest
+import torch
+
+import oracle as O
+from bitwise_spgemm_gb300 import capi, ops
+from bitwise_spgemm_gb300 import workloads as W
+from gpu_util import bf16_dev
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-4
+
+
+def _problems(n, N, seed, integer=False, kmax=1024):
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        M = int(32 * rng.integers(1, 40))
+        K = int(32 * rng.integers(1, kmax // 32))
+        d = float(rng.uniform(0.01, 0.3))
+        words = W.pack_bits(rng.random((M, K)) < d)
+        Bf = (rng.integers(-8, 9, (K, N)) if integer else rng.standard_normal((K, N))).astype(np.float32)
+        b16 = W.f32_to_bf16_bits(Bf)
+        out.append((words, K, b16))
+    return out
+
+
+def _run(probs, N):
+    dev = []
+    for words, K, b16 in probs:
+        wd = torch.from_numpy(np.ascontiguousarray(words).view(np.int32)).cuda()
+        dev.append((wd, K, bf16_dev(b16), torch.full((words.shape[0], N), float("nan"), device="cuda")))
+    return dev
+
+
+@pytest.mark.parametrize("N", [128, 200, 520])
+def test_batched_matches_oracle(N):
+    probs = _problems(24, N, seed=N)
+    dev = _run(probs, N)
+    batch = ops.Batch(dev)
+    batch.run()
+    torch.cuda.synchronize()
+    assert capi.device_status() == 0
+    for (words, K, b16), (_, _, _, Cd) in zip(probs, dev):
+        Bx = W.bf16_bits_to_f32(b16)
+        C = Cd.cpu().numpy()
+        mx, _, _ = O.rel_errors(C, O.spmm_f64(words, K, Bx), O.spmm_abs_f64(words, K, Bx))
+        assert mx <= TOL
+
+
+def test_batched_integer_exact_and_graph_replay():
+    N = 128
+    probs = _problems(16, N, seed=5, integer=True)
+    dev = _run(probs, N)
+    batch = ops.Batch(dev)
+    batch.run()  # first run outside capture
+    torch.cuda.synchronize()
+    for _, _, _, Cd in dev:
+        Cd.fill_(float("nan"))
+    g = torch.cuda.CUDAGraph()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(g, stream=s):
+            batch.run()
+    g.replay()
+    g.replay()
+    torch.cuda.synchronize()
+    assert capi.device_status() == 0
+    for (words, K, b16), (_, _, _, Cd) in zip(probs, dev):
+        assert np.array_equal(Cd.cpu().numpy().astype(np.float64), O.spmm_f64(words, K, W.bf16_bits_to_f32(b16)))
+
+
+def test_batched_empty_reduction_and_validation():
+    N = 128
+    wd = torch.zeros((64, 0), dtype=torch.int32, device="cuda")
+    Bz = torch.zeros((0, N), dtype=torch.bfloat16, device="cuda")
+    Cz = torch.full((64, N), 3.0, device="cuda")
+    probs = _problems(3, N, seed=9)
+    dev = _run(probs, N) + [(wd, 0, Bz, Cz)]
+    batch = ops.Batch(dev)
+    batch.run()
+    torch.cuda.synchronize()
+    assert torch.all(Cz == 0)
+    # FP32 B is not a batch type; N not a multiple of 8 is refused
+    with pytest.raises(capi.BspError):
+        ops.Batch([(dev[0][0], dev[0][1], dev[0][2].float(), dev[0][3])])
+    Bodd = torch.zeros((dev[0][1], 12), dtype=torch.bfloat16, device="cuda")
+    with pytest.raises(capi.BspError):
+        ops.Batch([(dev[0][0], dev[0][1], Bodd, torch.zeros((dev[0][0].shape[0], 12), device="cuda"))])
