@@ -145,6 +145,19 @@ __device__ __forceinline__ void cp_async_wait_group() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
+// 2-D TMA tensor copy global -> shared of one box at coordinates (x, y)
+// (x innermost, in elements; x * element size must be a multiple of 16
+// bytes), completing as transaction bytes on `bar`.  `map` is the address of
+// a __grid_constant__ CUtensorMap kernel parameter.  Boxes reaching past the
+// tensor are zero-filled.
+__device__ __forceinline__ void tma_load_2d(void* dst_smem, const void* map, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_addr(dst_smem)),
+      "l"(map), "r"(x), "r"(y), "r"(smem_addr(bar))
+      : "memory");
+}
+
 // Shared-memory matrix descriptor (tcgen05), no swizzle: start address,
 // leading-dimension byte offset, stride byte offset (all >> 4), version 1.
 __device__ __forceinline__ uint64_t smem_desc_noswizzle(const void* p, uint32_t lbo, uint32_t sbo) {

@@ -19,6 +19,11 @@
 //     stage and commits them to the stage's "empty" mbarrier.
 // Four stages of 24 KB; every mbarrier wait is bounded (timeout → error 3
 // in g_tc_error, the CTA skips to freeing its TMEM).
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <cstdlib>
+#include <cstring>
 #include <type_traits>
 
 #include "ptx.cuh"
@@ -34,7 +39,7 @@ namespace {
 constexpr int kTcM = 128;
 constexpr int kTcN = 256;
 constexpr int kTcK = 32;
-constexpr int kStages = 4;
+constexpr int kLook = 8;  // A words are loaded this many K tiles ahead
 constexpr int kAStage = kTcM * kTcK * 2;  // 8 KB
 constexpr int kBStage = kTcK * kTcN * 2;  // 16 KB
 constexpr int kProducers = 128;
@@ -49,7 +54,11 @@ using tc::kLbo;
 using tc::kSbo;
 using tc::expand8;
 constexpr int kFwd = 0, kTrans = 1, kSddmm = 2;
+// SDDMM operands arrive by TMA as columns of core matrices: the 8-column
+// K slices of the 128-row G tile are kSdA apart, of the 256-row X tile kSdB.
+constexpr uint32_t kSdA = 128 * 16, kSdB = 256 * 16;
 
+template <int kStages>
 struct __align__(1024) TcSmem {
   uint8_t a[kStages][kAStage];
   uint8_t b[kStages][kBStage];
@@ -129,10 +138,11 @@ struct StepIter {
 // All three use the same core-matrix geometry (LBO = 128 B along the
 // reduction, SBO = 512 B along M/N) and differ only in the producers, the
 // instruction descriptor's major bits and the epilogue.
-template <typename BT, int MODE>
-__global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a) {
+template <typename BT, int MODE, int kStages>
+__global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __grid_constant__ CUtensorMap mapA,
+                                                          const __grid_constant__ CUtensorMap mapB) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
-  TcSmem& sm = *reinterpret_cast<TcSmem*>(smem_raw);
+  TcSmem<kStages>& sm = *reinterpret_cast<TcSmem<kStages>*>(smem_raw);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int64_t row0 = (int64_t)blockIdx.x * kTcM;  // output rows: M (fwd, sddmm) or K (trans)
   const int64_t col0 = (int64_t)blockIdx.y * kTcN;  // output columns: N (fwd, trans) or K (sddmm)
@@ -142,7 +152,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a) {
 
   if (tid == 0) {
     for (int s = 0; s < kStages; s++) {
-      ptx::mbar_init(&sm.full[s], kProducers);
+      ptx::mbar_init(&sm.full[s], kProducers + 1);  // producers + the TMA transaction arrival
       ptx::mbar_init(&sm.empty[s], 1);
     }
     ptx::mbar_init(&sm.done, 1);
@@ -173,12 +183,34 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a) {
 
   if (warp < 4) {
     // ---------------- producers ----------------
-    const BT* __restrict__ Bsrc = static_cast<const BT*>(a.B);
-    const BT* __restrict__ Gsrc = static_cast<const BT*>(a.G);
+    // Operands that are dense 16-bit tiles come by TMA (warp 0 issues the
+    // boxes and the stage's transaction count); the bit tiles of A are
+    // expanded by all 128 producers from words loaded two tiles ahead.
     StepIter it;
     it.init(block_occ, a.occ_words, dense_steps, MODE == kSddmm);
+    auto load_word = [&](int t) -> uint32_t {
+      if (t < 0 || MODE == kSddmm) return 0u;
+      if (MODE == kFwd) {
+        const int64_t arow = row0 + tid;
+        return arow < a.M ? __ldg(a.A + arow * a.Kw + t) : 0u;
+      }
+      const int64_t arow = (int64_t)t * kTcK + (tid & 31);
+      const int64_t wcol = row0 / 32 + (tid >> 5);
+      return (arow < a.M && wcol < a.Kw) ? __ldg(a.A + arow * a.Kw + wcol) : 0u;
+    };
+    // tq[0] is the current tile, tq[1..kLook] the next ones; wq[j] holds the
+    // A word of tq[j] (loads issued kLook tiles before use)
+    int tq[kLook + 1];
+    uint32_t wq[kLook];
+#pragma unroll
+    for (int j = 0; j <= kLook; j++) tq[j] = (j == 0 || tq[j - 1] >= 0) ? it.next() : -1;
+#pragma unroll
+    for (int j = 0; j < kLook; j++) wq[j] = load_word(tq[j]);
     int i = 0;
-    for (int t = it.next(); t >= 0; t = it.next(), i++) {
+    for (; tq[0] >= 0; i++) {
+      const int t0 = tq[0];
+      const uint32_t w0 = wq[0];
+      const uint32_t wnew = load_word(tq[kLook]);
       const int s = i % kStages;
       if (i >= kStages && !ptx::mbar_wait(&sm.empty[s], ((i / kStages) - 1) & 1)) {
         atomicCAS(&g_tc_error, 0, 3);
@@ -186,75 +218,42 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a) {
         break;
       }
       if (*(volatile int*)&sm.abort) break;
+      if (warp == 0) {
+        if (lane == 0) ptx::mbar_arrive_expect_tx(&sm.full[s], MODE == kSddmm ? kAStage + kBStage : kBStage);
+        __syncwarp();
+        if (MODE == kSddmm) {
+          // G rows row0.. and X rows col0.., columns t0*32 + 8*j: K-major
+          // columns of core matrices (row r at 16*r), one box per 8 columns
+          if (lane < 4)
+            ptx::tma_load_2d(sm.a[s] + lane * kSdA, &mapA, t0 * kTcK + lane * 8, (int)row0, &sm.full[s]);
+          else if (lane < 8)
+            ptx::tma_load_2d(sm.b[s] + (lane - 4) * kSdB, &mapB, t0 * kTcK + (lane - 4) * 8, (int)col0, &sm.full[s]);
+        } else {
+          // B (fwd) / G (trans): reduction rows t0*32.., columns col0 + 8*lane
+          ptx::tma_load_2d(sm.b[s] + lane * kSbo, &mapB, (int)col0 + lane * 8, t0 * kTcK, &sm.full[s]);
+        }
+      }
       if (MODE == kFwd) {
-        // A: row tid's word t → 4 core-matrix rows (K-major)
-        const int64_t arow = row0 + tid;
-        const uint32_t w = arow < a.M ? __ldg(a.A + arow * a.Kw + t) : 0u;
         uint8_t* as = sm.a[s] + (tid >> 3) * kSbo + (tid & 7) * 16;
 #pragma unroll
-        for (int c = 0; c < 4; c++) *reinterpret_cast<uint4*>(as + c * kLbo) = expand8((w >> (8 * c)) & 0xffu, one);
+        for (int c = 0; c < 4; c++) *reinterpret_cast<uint4*>(as + c * kLbo) = expand8((w0 >> (8 * c)) & 0xffu, one);
       } else if (MODE == kTrans) {
-        // Aᵀ: row j of the 32-row tile, word wk of the 128-column block →
-        // 4 core-matrix rows of the MN-major operand
         const int j = tid & 31, wk = tid >> 5;
-        const int64_t arow = (int64_t)t * kTcK + j;
-        const int64_t wcol = row0 / 32 + wk;
-        const uint32_t w = (arow < a.M && wcol < a.Kw) ? __ldg(a.A + arow * a.Kw + wcol) : 0u;
         uint8_t* as = sm.a[s] + (j >> 3) * kLbo + (j & 7) * 16;
 #pragma unroll
         for (int c = 0; c < 4; c++)
-          *reinterpret_cast<uint4*>(as + (wk * 4 + c) * kSbo) = expand8((w >> (8 * c)) & 0xffu, one);
-      } else {
-        // G tile: rows row0.., columns t*32.. (K-major), 512 chunks
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-          const int q = tid + kProducers * j;
-          const int m = q >> 2, k8 = q & 3;
-          const int64_t r = row0 + m;
-          const int64_t c = (int64_t)t * kTcK + k8 * 8;
-          const bool ok = r < a.M && c < a.N;
-          ptx::cp_async_16(sm.a[s] + (m >> 3) * kSbo + k8 * kLbo + (m & 7) * 16,
-                           ok ? Gsrc + r * a.ldg + c : Gsrc, ok ? 16u : 0u);
-        }
+          *reinterpret_cast<uint4*>(as + (wk * 4 + c) * kSbo) = expand8((w0 >> (8 * c)) & 0xffu, one);
       }
-      if (MODE == kSddmm) {
-        // X tile: rows col0.. (columns of dA), columns t*32.. (K-major), 1024 chunks
+      ptx::fence_proxy_async_smem();
+      ptx::mbar_arrive(&sm.full[s]);
 #pragma unroll
-        for (int j = 0; j < 8; j++) {
-          const int q = tid + kProducers * j;
-          const int nn = q >> 2, k8 = q & 3;
-          const int64_t r = col0 + nn;
-          const int64_t c = (int64_t)t * kTcK + k8 * 8;
-          const bool ok = r < a.K && c < a.N;
-          ptx::cp_async_16(sm.b[s] + (nn >> 3) * kSbo + k8 * kLbo + (nn & 7) * 16,
-                           ok ? Bsrc + r * a.ldb + c : Bsrc, ok ? 16u : 0u);
-        }
-      } else {
-        // B (fwd) / G (trans) tile: reduction rows t*32.., columns col0.. (MN-major)
-        const int64_t red_limit = MODE == kFwd ? a.K : a.M;
+      for (int j = 0; j < kLook - 1; j++) wq[j] = wq[j + 1];
+      wq[kLook - 1] = wnew;
 #pragma unroll
-        for (int j = 0; j < 8; j++) {
-          const int q = tid + kProducers * j;
-          const int k = q >> 5, n8 = q & 31;
-          const int64_t krow = (int64_t)t * kTcK + k;
-          const int64_t ncol = col0 + n8 * 8;
-          const bool ok = krow < red_limit && ncol < a.N;
-          ptx::cp_async_16(sm.b[s] + n8 * kSbo + (k >> 3) * kLbo + (k & 7) * 16,
-                           ok ? Bsrc + krow * a.ldb + ncol : Bsrc, ok ? 16u : 0u);
-        }
-      }
-      ptx::cp_async_commit();
-      // step i-2 is now complete: publish it to the MMA issuer
-      ptx::cp_async_wait_group<2>();
-      if (i >= 2) {
-        ptx::fence_proxy_async_smem();
-        ptx::mbar_arrive(&sm.full[(i - 2) % kStages]);
-      }
+      for (int j = 0; j < kLook; j++) tq[j] = tq[j + 1];
+      tq[kLook] = tq[kLook] >= 0 ? it.next() : -1;
     }
     ntiles = i;
-    ptx::cp_async_wait_group<0>();
-    ptx::fence_proxy_async_smem();
-    for (int j = (ntiles >= 2 ? ntiles - 2 : 0); j < ntiles; j++) ptx::mbar_arrive(&sm.full[j % kStages]);
   } else if (lane == 0) {
     // ---------------- MMA issuer ----------------
     const uint32_t ab = std::is_same<BT, __nv_bfloat16>::value ? 1u : 0u;
@@ -273,8 +272,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a) {
       ptx::tc_fence_after_sync();
 #pragma unroll
       for (int j = 0; j < 2; j++) {
-        const uint64_t ad = ptx::smem_desc_noswizzle(sm.a[s] + j * 2 * kLbo, kLbo, kSbo);
-        const uint64_t bd = ptx::smem_desc_noswizzle(sm.b[s] + j * 2 * kLbo, kLbo, kSbo);
+        uint64_t ad, bd;
+        if (MODE == kSddmm) {  // TMA layout: core-matrix columns of 128 / 256 rows
+          ad = ptx::smem_desc_noswizzle(sm.a[s] + j * 2 * kSdA, kSdA, 128);
+          bd = ptx::smem_desc_noswizzle(sm.b[s] + j * 2 * kSdB, kSdB, 128);
+        } else {
+          ad = ptx::smem_desc_noswizzle(sm.a[s] + j * 2 * kLbo, kLbo, kSbo);
+          bd = ptx::smem_desc_noswizzle(sm.b[s] + j * 2 * kLbo, kLbo, kSbo);
+        }
         ptx::tc_mma_f16(tmem, ad, bd, idesc, (i > 0) || (j > 0));
       }
       ptx::tc_commit(&sm.empty[s]);
@@ -408,19 +413,73 @@ int launch_tile_occupancy_t(const uint32_t* A, int64_t M, int64_t K, uint32_t* o
 }
 
 namespace {
-template <typename BT, int MODE>
-int launch_mode(const TcArgs& a, dim3 grid, cudaStream_t s) {
-  const size_t smem = sizeof(TcSmem);
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no
+// link-time dependency on the driver library).
+PFN_cuTensorMapEncodeTiled_v12000 encode_tiled() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+// 2-D map over a row-major [rows][cols] 16-bit matrix (row stride ld
+// elements), box = box_cols x box_rows, no swizzle, out-of-range = zero.
+int make_map(CUtensorMap* m, const void* base, int dt, int64_t rows, int64_t cols, int64_t ld, uint32_t box_cols,
+             uint32_t box_rows) {
+  PFN_cuTensorMapEncodeTiled_v12000 enc = encode_tiled();
+  if (!enc) return BSP_ERR_UNSUPPORTED;
+  const cuuint64_t dims[2] = {(cuuint64_t)(cols > 0 ? cols : 1), (cuuint64_t)(rows > 0 ? rows : 1)};
+  const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+  const cuuint32_t box[2] = {box_cols, box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = enc(m, dt == BSP_BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2,
+                         const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                         CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? BSP_OK : BSP_ERR_ALIGNMENT;
+}
+
+template <typename BT, int MODE, int S>
+int launch_stages(const TcArgs& a, const CUtensorMap& ma, const CUtensorMap& mb, dim3 grid, cudaStream_t s) {
+  const size_t smem = sizeof(TcSmem<S>);
   static bool configured[64] = {};
   int dev = 0;
   BSP_CUDA(cudaGetDevice(&dev));
   if (dev < 64 && !configured[dev]) {
-    BSP_CUDA(cudaFuncSetAttribute(k_spmm_tc<BT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    BSP_CUDA(cudaFuncSetAttribute(k_spmm_tc<BT, MODE, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     configured[dev] = true;
   }
-  k_spmm_tc<BT, MODE><<<grid, kTcThreads, smem, s>>>(a);
+  k_spmm_tc<BT, MODE, S><<<grid, kTcThreads, smem, s>>>(a, ma, mb);
   BSP_LAUNCHED();
   return BSP_OK;
+}
+
+// Stage ring depth: 4 stages (two CTAs per SM) or 6 / 8 (one CTA per SM);
+// BSP_TC_STAGES selects it for tuning.
+int tc_stages() {
+  static int v = 0;
+  if (!v) {
+    const char* e = getenv("BSP_TC_STAGES");
+    v = e ? atoi(e) : 4;
+    if (v != 4 && v != 6 && v != 8) v = 4;
+  }
+  return v;
+}
+
+template <typename BT, int MODE>
+int launch_mode(const TcArgs& a, const CUtensorMap& ma, const CUtensorMap& mb, dim3 grid, cudaStream_t s) {
+  switch (tc_stages()) {
+    case 6: return launch_stages<BT, MODE, 6>(a, ma, mb, grid, s);
+    case 8: return launch_stages<BT, MODE, 8>(a, ma, mb, grid, s);
+    default: return launch_stages<BT, MODE, 4>(a, ma, mb, grid, s);
+  }
 }
 
 template <int MODE>
@@ -430,8 +489,18 @@ int launch_tc(const TcArgs& a, cudaStream_t s) {
   if (rows == 0 || cols == 0) return BSP_OK;
   const dim3 grid((unsigned)ceil_div(rows, kTcM), (unsigned)ceil_div(cols, kTcN));
   if (ceil_div(cols, kTcN) > 65535 || ceil_div(rows, kTcM) > 0x7fffffff) return BSP_ERR_CAPACITY;
-  if (a.bdt == BSP_BF16) return launch_mode<__nv_bfloat16, MODE>(a, grid, s);
-  if (a.bdt == BSP_F16) return launch_mode<__half, MODE>(a, grid, s);
+  if (a.N > INT32_MAX || a.M > INT32_MAX || a.K > INT32_MAX) return BSP_ERR_CAPACITY;
+  CUtensorMap ma, mb;
+  memset(&ma, 0, sizeof(ma));
+  if (MODE == kSddmm) {
+    BSP_TRY(make_map(&ma, a.G, a.bdt, a.M, a.N, a.ldg, 8, kTcM));  // G [M][N]
+    BSP_TRY(make_map(&mb, a.B, a.bdt, a.K, a.N, a.ldb, 8, kTcN));  // X [K][N]
+  } else {
+    // B [K][N] (fwd) or G [M][N] (trans), 32 reduction rows per box
+    BSP_TRY(make_map(&mb, a.B, a.bdt, MODE == kFwd ? a.K : a.M, a.N, a.ldb, 8, kTcK));
+  }
+  if (a.bdt == BSP_BF16) return launch_mode<__nv_bfloat16, MODE>(a, ma, mb, grid, s);
+  if (a.bdt == BSP_F16) return launch_mode<__half, MODE>(a, ma, mb, grid, s);
   return BSP_ERR_UNSUPPORTED;
 }
 }  // namespace
