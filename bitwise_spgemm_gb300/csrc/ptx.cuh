@@ -166,5 +166,12 @@ __device__ __forceinline__ uint64_t smem_desc_noswizzle(const void* p, uint32_t 
          (1ull << 46);
 }
 
+// Swizzled descriptor: layout 2 = 128-byte swizzle, 4 = 64-byte, 6 = 32-byte
+// (bits 61-63); the swizzle atoms must sit at addresses aligned to their size
+// (1024 / 512 / 256 bytes), so the base-offset field stays 0.
+__device__ __forceinline__ uint64_t smem_desc_swizzle(const void* p, uint32_t lbo, uint32_t sbo, uint32_t layout) {
+  return smem_desc_noswizzle(p, lbo, sbo) | ((uint64_t)layout << 61);
+}
+
 }  // namespace ptx
 }  // namespace bsp

@@ -12,9 +12,10 @@
 // the K tiles where some row of the 128-row block has a set bit (the plan's
 // occupancy bitmap), so empty bit tiles cost nothing.
 //   warps 0-3 (producers): expand the 128 words of the stage into the A
-//     operand (K-major core-matrix layout) and stream the 32x256 B tile with
-//     16-byte cp.async into the MN-major core-matrix layout; then, after the
-//     last stage, read the accumulator back with tcgen05.ld and store C;
+//     operand (K-major core-matrix layout); warp 0 also issues the stage's
+//     B tile as four 64x32 TMA boxes in the 128-byte-swizzled MN-major
+//     layout; then, after the last stage, read the accumulator back with
+//     tcgen05.ld and store C;
 //   warp 4: allocates TMEM; its lane 0 issues two tcgen05.mma (K=16) per
 //     stage and commits them to the stage's "empty" mbarrier.
 // Four stages of 24 KB; every mbarrier wait is bounded (timeout → error 3
@@ -53,10 +54,19 @@ constexpr uint32_t kTmemCols = kGuard ? 512 : 256;
 using tc::kLbo;
 using tc::kSbo;
 using tc::expand8;
+using tc::kLayoutSw128;
+using tc::kLayoutSw64;
 constexpr int kFwd = 0, kTrans = 1, kSddmm = 2;
-// SDDMM operands arrive by TMA as columns of core matrices: the 8-column
-// K slices of the 128-row G tile are kSdA apart, of the 256-row X tile kSdB.
-constexpr uint32_t kSdA = 128 * 16, kSdB = 256 * 16;
+// B (fwd) / G (trans) tile: four TMA boxes of 64 columns x 32 reduction rows,
+// 128-byte swizzle, kBox bytes apart (the LBO); 8-row groups 1 KB apart (SBO).
+constexpr int kBoxCols = 64;
+constexpr uint32_t kBox = kBoxCols * kTcK * 2;  // 4 KB
+// SDDMM: G tile 128 rows x 32 (of N) and X tile 256 rows x 32 (of N), one
+// box each, K-major with 64-byte swizzle (8-row groups 512 B apart).
+constexpr uint32_t kSdSbo = 512;
+// Shared memory is requested with this much slack so the stage buffers can
+// be aligned to the 1 KB swizzle atom.
+constexpr size_t kSmemAlign = 1024;
 
 template <int kStages>
 struct __align__(1024) TcSmem {
@@ -133,16 +143,18 @@ struct StepIter {
 //   kFwd   C[M,N]  = A · B        A bits K-major from A's words, B MN-major
 //   kTrans C[K,N]  = Aᵀ · G       Aᵀ MN-major built from A's row words (no
 //                                 transposed copy), G MN-major
-//   kSddmm dA[M,K] = (G · Xᵀ) ⊙ A  G and X K-major (16-byte cp.async),
+//   kSddmm dA[M,K] = (G · Xᵀ) ⊙ A  G and X K-major (TMA, 64-byte swizzle),
 //                                 dense over N, masked store
-// All three use the same core-matrix geometry (LBO = 128 B along the
-// reduction, SBO = 512 B along M/N) and differ only in the producers, the
-// instruction descriptor's major bits and the epilogue.
+// The bit operands are expanded into core matrices (LBO = 128 B along the
+// reduction, SBO = 512 B along M/N); the dense 16-bit operands come by TMA
+// in swizzled layouts.  The modes differ only in the producers, the
+// descriptors and the epilogue.
 template <typename BT, int MODE, int kStages>
 __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __grid_constant__ CUtensorMap mapA,
                                                           const __grid_constant__ CUtensorMap mapB) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
-  TcSmem<kStages>& sm = *reinterpret_cast<TcSmem<kStages>*>(smem_raw);
+  TcSmem<kStages>& sm = *reinterpret_cast<TcSmem<kStages>*>(
+      smem_raw + ((kSmemAlign - (ptx::smem_addr(smem_raw) & (kSmemAlign - 1))) & (kSmemAlign - 1)));
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int64_t row0 = (int64_t)blockIdx.x * kTcM;  // output rows: M (fwd, sddmm) or K (trans)
   const int64_t col0 = (int64_t)blockIdx.y * kTcN;  // output columns: N (fwd, trans) or K (sddmm)
@@ -222,15 +234,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
         if (lane == 0) ptx::mbar_arrive_expect_tx(&sm.full[s], MODE == kSddmm ? kAStage + kBStage : kBStage);
         __syncwarp();
         if (MODE == kSddmm) {
-          // G rows row0.. and X rows col0.., columns t0*32 + 8*j: K-major
-          // columns of core matrices (row r at 16*r), one box per 8 columns
-          if (lane < 4)
-            ptx::tma_load_2d(sm.a[s] + lane * kSdA, &mapA, t0 * kTcK + lane * 8, (int)row0, &sm.full[s]);
-          else if (lane < 8)
-            ptx::tma_load_2d(sm.b[s] + (lane - 4) * kSdB, &mapB, t0 * kTcK + (lane - 4) * 8, (int)col0, &sm.full[s]);
-        } else {
-          // B (fwd) / G (trans): reduction rows t0*32.., columns col0 + 8*lane
-          ptx::tma_load_2d(sm.b[s] + lane * kSbo, &mapB, (int)col0 + lane * 8, t0 * kTcK, &sm.full[s]);
+          // G rows row0.. and X rows col0.., columns t0*32..: one box each
+          if (lane == 0) ptx::tma_load_2d(sm.a[s], &mapA, t0 * kTcK, (int)row0, &sm.full[s]);
+          else if (lane == 1) ptx::tma_load_2d(sm.b[s], &mapB, t0 * kTcK, (int)col0, &sm.full[s]);
+        } else if (lane < kTcN / kBoxCols) {
+          // B (fwd) / G (trans): reduction rows t0*32.., columns col0 + 64*lane
+          ptx::tma_load_2d(sm.b[s] + lane * kBox, &mapB, (int)col0 + lane * kBoxCols, t0 * kTcK, &sm.full[s]);
         }
       }
       if (MODE == kFwd) {
@@ -273,12 +282,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
 #pragma unroll
       for (int j = 0; j < 2; j++) {
         uint64_t ad, bd;
-        if (MODE == kSddmm) {  // TMA layout: core-matrix columns of 128 / 256 rows
-          ad = ptx::smem_desc_noswizzle(sm.a[s] + j * 2 * kSdA, kSdA, 128);
-          bd = ptx::smem_desc_noswizzle(sm.b[s] + j * 2 * kSdB, kSdB, 128);
-        } else {
+        if (MODE == kSddmm) {  // both K-major, 64-byte swizzle; K half j starts 32 B in
+          ad = ptx::smem_desc_swizzle(sm.a[s] + j * 32, 16, kSdSbo, kLayoutSw64);
+          bd = ptx::smem_desc_swizzle(sm.b[s] + j * 32, 16, kSdSbo, kLayoutSw64);
+        } else {  // A: core matrices; B: 128-byte swizzle, K half j = two 8-row groups on
           ad = ptx::smem_desc_noswizzle(sm.a[s] + j * 2 * kLbo, kLbo, kSbo);
-          bd = ptx::smem_desc_noswizzle(sm.b[s] + j * 2 * kLbo, kLbo, kSbo);
+          bd = ptx::smem_desc_swizzle(sm.b[s] + j * 2 * 1024, kBox, 1024, kLayoutSw128);
         }
         ptx::tc_mma_f16(tmem, ad, bd, idesc, (i > 0) || (j > 0));
       }
@@ -430,9 +439,9 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_tiled() {
 }
 
 // 2-D map over a row-major [rows][cols] 16-bit matrix (row stride ld
-// elements), box = box_cols x box_rows, no swizzle, out-of-range = zero.
+// elements), box = box_cols x box_rows, out-of-range = zero.
 int make_map(CUtensorMap* m, const void* base, int dt, int64_t rows, int64_t cols, int64_t ld, uint32_t box_cols,
-             uint32_t box_rows) {
+             uint32_t box_rows, CUtensorMapSwizzle swz) {
   PFN_cuTensorMapEncodeTiled_v12000 enc = encode_tiled();
   if (!enc) return BSP_ERR_UNSUPPORTED;
   const cuuint64_t dims[2] = {(cuuint64_t)(cols > 0 ? cols : 1), (cuuint64_t)(rows > 0 ? rows : 1)};
@@ -441,14 +450,14 @@ int make_map(CUtensorMap* m, const void* base, int dt, int64_t rows, int64_t col
   const cuuint32_t estr[2] = {1, 1};
   const CUresult r = enc(m, dt == BSP_BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2,
                          const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                         CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                         swz, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? BSP_OK : BSP_ERR_ALIGNMENT;
 }
 
 template <typename BT, int MODE, int S>
 int launch_stages(const TcArgs& a, const CUtensorMap& ma, const CUtensorMap& mb, dim3 grid, cudaStream_t s) {
-  const size_t smem = sizeof(TcSmem<S>);
+  const size_t smem = sizeof(TcSmem<S>) + kSmemAlign;
   static bool configured[64] = {};
   int dev = 0;
   BSP_CUDA(cudaGetDevice(&dev));
@@ -493,11 +502,12 @@ int launch_tc(const TcArgs& a, cudaStream_t s) {
   CUtensorMap ma, mb;
   memset(&ma, 0, sizeof(ma));
   if (MODE == kSddmm) {
-    BSP_TRY(make_map(&ma, a.G, a.bdt, a.M, a.N, a.ldg, 8, kTcM));  // G [M][N]
-    BSP_TRY(make_map(&mb, a.B, a.bdt, a.K, a.N, a.ldb, 8, kTcN));  // X [K][N]
+    BSP_TRY(make_map(&ma, a.G, a.bdt, a.M, a.N, a.ldg, kTcK, kTcM, CU_TENSOR_MAP_SWIZZLE_64B));  // G [M][N]
+    BSP_TRY(make_map(&mb, a.B, a.bdt, a.K, a.N, a.ldb, kTcK, kTcN, CU_TENSOR_MAP_SWIZZLE_64B));  // X [K][N]
   } else {
-    // B [K][N] (fwd) or G [M][N] (trans), 32 reduction rows per box
-    BSP_TRY(make_map(&mb, a.B, a.bdt, MODE == kFwd ? a.K : a.M, a.N, a.ldb, 8, kTcK));
+    // B [K][N] (fwd) or G [M][N] (trans), 64 columns x 32 reduction rows per box
+    BSP_TRY(make_map(&mb, a.B, a.bdt, MODE == kFwd ? a.K : a.M, a.N, a.ldb, kBoxCols, kTcK,
+                     CU_TENSOR_MAP_SWIZZLE_128B));
   }
   if (a.bdt == BSP_BF16) return launch_mode<__nv_bfloat16, MODE>(a, ma, mb, grid, s);
   if (a.bdt == BSP_F16) return launch_mode<__half, MODE>(a, ma, mb, grid, s);

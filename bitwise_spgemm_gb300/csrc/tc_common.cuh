@@ -15,6 +15,19 @@ namespace tc {
 //   MN-major: element (k, mn) at (mn/8)*kSbo + (k/8)*kLbo + (k%8)*16 + (mn%8)*2
 constexpr uint32_t kLbo = 128, kSbo = 512;
 
+// Dense 16-bit operands that arrive by TMA use swizzled layouts instead: a
+// box of 16-byte rows moves at about a quarter of the L2 -> shared memory
+// rate of 128-byte rows (measured on GB300: 2.4 vs 7-9 TB/s).
+//   MN-major, 128-byte swizzle: atoms of 8 reduction rows x 64 elements
+//     (1024 B, rows 128 B apart, 16-byte chunk q of row r stored at chunk
+//     q ^ (r & 7)); SBO = distance between 8-row groups along the reduction,
+//     LBO = distance between 64-element atoms along M / N.
+//   K-major, 64-byte swizzle: atoms of 8 rows x 32 reduction elements (512 B,
+//     chunk q of row r at q ^ ((r >> 1) & 3)); SBO = distance between 8-row
+//     groups, LBO unused; the second K=16 half starts 32 bytes in.
+constexpr uint32_t kLayoutSw128 = 2, kLayoutSw64 = 4;
+constexpr uint32_t kSw128Atom = 1024, kSw64Atom = 512;
+
 // Instruction descriptor for kind::f16: D f32 (bits 4-5), A and B of the
 // same 16-bit type (bits 7-9, 10-12: bf16 = 1, f16 = 0), A / B major (bits
 // 15, 16: 0 = K-major, 1 = MN-major), N >> 3 (bits 17-22), M >> 4 (24-28).
