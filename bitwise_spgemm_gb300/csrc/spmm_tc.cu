@@ -7,19 +7,25 @@
 // source/src/mm.cu:123-145, which expanded 8x8 bitmap tiles into 0/1 half
 // wmma fragments) and multiplied by the matching 32 rows of B.
 //
-// CTA tile: 128 rows x 256 columns of C, FP32 accumulator in TMEM (256
-// columns).  K advances 32 columns (one packed word) per stage, and only over
-// the K tiles where some row of the 128-row block has a set bit (the plan's
-// occupancy bitmap), so empty bit tiles cost nothing.
-//   warps 0-3 (producers): expand the 128 words of the stage into the A
-//     operand (K-major core-matrix layout); warp 0 also issues the stage's
-//     B tile as four 64x32 TMA boxes in the 128-byte-swizzled MN-major
-//     layout; then, after the last stage, read the accumulator back with
-//     tcgen05.ld and store C;
-//   warp 4: allocates TMEM; its lane 0 issues two tcgen05.mma (K=16) per
-//     stage and commits them to the stage's "empty" mbarrier.
-// Four stages of 24 KB; every mbarrier wait is bounded (timeout → error 3
-// in g_tc_error, the CTA skips to freeing its TMEM).
+// CTA tile: 256 rows x 256 columns of C as two 128-row halves, each with its
+// FP32 accumulator in TMEM (2 x 256 columns); both halves multiply the same
+// B stage, so every B byte brought into shared memory feeds 256 rows.  K
+// advances 32 columns (one packed word) per stage, over the K tiles where
+// either 128-row block has a set bit (the plan's occupancy bitmap, one per
+// 128-row block); a half without bits in the tile skips its MMAs.
+//   warps 0-7 (A producers): expand the words of the stage's two K tiles
+//     into the A operand (K-major core-matrix layout, one row per thread);
+//     after the last stage they read the accumulators back with tcgen05.ld
+//     and store C;
+//   warp 8 (TMA): issues the B rows of the stage's tiles as 64x32 boxes in
+//     the 128-byte-swizzled MN-major layout;
+//   warp 9: allocates TMEM; its lane 0 issues two tcgen05.mma (K=16) per
+//     occupied half per tile and commits the stage to its "empty" mbarrier.
+// An mbarrier hand-off costs 200-400 cycles on GB300 whatever the waiting
+// form, so a stage carries two tiles (up to eight MMAs, ~1000 cycles of
+// tensor work) per wait and per commit.  Three stages of 64 KB; every
+// mbarrier wait is bounded (timeout → error 3 in g_tc_error, the CTA skips to
+// freeing its TMEM).
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -37,47 +43,50 @@ __device__ int g_tc_error;
 
 namespace {
 
-constexpr int kTcM = 128;
+constexpr int kTcM = 128;                 // rows of one MMA and of one occupancy block
+constexpr int kHalves = 2;                // a CTA owns two 128-row halves ...
+constexpr int kCtaM = kTcM * kHalves;     // ... 256 output rows, sharing every B tile
 constexpr int kTcN = 256;
-constexpr int kTcK = 32;
-constexpr int kLook = 8;  // A words are loaded this many K tiles ahead
-constexpr int kAStage = kTcM * kTcK * 2;  // 8 KB
-constexpr int kBStage = kTcK * kTcN * 2;  // 16 KB
-constexpr int kProducers = 128;
-constexpr int kTcThreads = 160;
-// kGuard: extra shared memory past the stage buffers and a full 512-column
-// TMEM allocation, so that a misread descriptor field cannot reach memory
-// the CTA does not own (used for the first bring-up of a descriptor change;
-// costs one CTA per SM).
-constexpr bool kGuard = false;
-constexpr uint32_t kTmemCols = kGuard ? 512 : 256;
+constexpr int kTcK = 32;                  // one packed word of A per row and K tile
+constexpr int kTilesPerStage = 2;         // a stage carries two occupied K tiles
+constexpr int kLook = 8;                  // A words are loaded this many K tiles ahead
+constexpr int kATile = kCtaM * kTcK * 2;  // 16 KB: both halves of one K tile
+constexpr int kAHalf = kTcM * kTcK * 2;   // 8 KB
+constexpr int kBTile = kTcK * kTcN * 2;   // 16 KB
+constexpr int kStageBytes = kTilesPerStage * kATile;  // per operand: 32 KB
+constexpr int kStages = 3;
+constexpr int kProducers = kCtaM;         // one producer thread per row of the CTA tile
+constexpr int kProducerWarps = kProducers / 32;
+constexpr int kTmaWarp = kProducerWarps;      // issues the TMA boxes
+constexpr int kMmaWarp = kProducerWarps + 1;  // allocates TMEM, issues the MMAs
+constexpr int kTcThreads = kProducers + 64;
+constexpr uint32_t kTmemCols = 512;       // two 128x256 FP32 accumulators
 using tc::kLbo;
 using tc::kSbo;
 using tc::expand8;
 using tc::kLayoutSw128;
-using tc::kLayoutSw64;
 constexpr int kFwd = 0, kTrans = 1, kSddmm = 2;
 // B (fwd) / G (trans) tile: four TMA boxes of 64 columns x 32 reduction rows,
 // 128-byte swizzle, kBox bytes apart (the LBO); 8-row groups 1 KB apart (SBO).
 constexpr int kBoxCols = 64;
 constexpr uint32_t kBox = kBoxCols * kTcK * 2;  // 4 KB
-// SDDMM: G tile 128 rows x 32 (of N) and X tile 256 rows x 32 (of N), one
-// box each, K-major with 64-byte swizzle (8-row groups 512 B apart).
-constexpr uint32_t kSdSbo = 512;
+// SDDMM: a stage is 64 columns of N: the G tile (256 rows) and the X tile
+// (256 rows) are one box each, K-major with 128-byte swizzle (rows 128 B,
+// 8-row groups 1 KB apart); the four K=16 steps start 32 B apart.
+constexpr int kSdK = 64;
+constexpr uint32_t kSdSbo = 1024;
 // Shared memory is requested with this much slack so the stage buffers can
 // be aligned to the 1 KB swizzle atom.
 constexpr size_t kSmemAlign = 1024;
 
-template <int kStages>
 struct __align__(1024) TcSmem {
-  uint8_t a[kStages][kAStage];
-  uint8_t b[kStages][kBStage];
-  uint64_t full[kStages];
-  uint64_t empty[kStages];
+  uint8_t a[kStages][kStageBytes];
+  uint8_t b[kStages][kStageBytes];
+  uint64_t full[kStages];   // producer warps + the TMA transaction arrival
+  uint64_t empty[kStages];  // tcgen05.commit of the stage's MMAs
   uint64_t done;
   uint32_t tmem_addr;
   int abort;
-  uint8_t guard[kGuard ? 65536 : 16];
 };
 
 __host__ __device__ constexpr uint32_t idesc_f16(uint32_t ab_type, uint32_t a_mn, uint32_t b_mn) {
@@ -99,43 +108,55 @@ struct TcArgs {
   int bdt;
 };
 
-struct TileIter {  // set bits of the block's occupancy words, ascending
-  const uint32_t* occ;
+// Occupied K tiles of the CTA's two 128-row blocks (forward: K tiles; trans:
+// row tiles of A), ascending over the union; `halves` tells which of the two
+// blocks have bits in the returned tile (bit 0 = first block).
+struct TileIter {
+  const uint32_t* o0;
+  const uint32_t* o1;  // null when the second block lies past the end
   int ow, nw;
-  uint32_t bits;
-  __device__ void init(const uint32_t* o, int n) {
-    occ = o;
+  uint32_t bits, b0, b1;
+  __device__ void init(const uint32_t* p0, const uint32_t* p1, int n) {
+    o0 = p0;
+    o1 = p1;
     nw = n;
     ow = -1;
-    bits = 0;
+    bits = b0 = b1 = 0;
   }
-  __device__ __forceinline__ int next() {
+  __device__ __forceinline__ int next(int& halves) {
     while (bits == 0) {
       if (++ow >= nw) return -1;
-      bits = __ldg(occ + ow);
+      b0 = __ldg(o0 + ow);
+      b1 = o1 ? __ldg(o1 + ow) : 0u;
+      bits = b0 | b1;
     }
     const int b = __ffs(bits) - 1;
     bits &= bits - 1;
+    halves = (int)(((b0 >> b) & 1u) | (((b1 >> b) & 1u) << 1));
     return ow * 32 + b;
   }
 };
 
-// Steps of the reduction: occupied tiles from a bitmap (forward: K tiles of
-// the CTA's 128-row block; transposed: row tiles of its 128-column block) or
-// every 32-column step of N (SDDMM).
+// Steps of the reduction: occupied tiles (forward / trans) or every
+// 32-column step of N (SDDMM, both halves unless the second is past the end).
 struct StepIter {
   TileIter it;
-  int dense_left, dense_i;
+  int dense_left, dense_i, dense_halves;
   bool dense;
-  __device__ void init(const uint32_t* occ, int words, int dense_steps, bool is_dense) {
+  __device__ void init(const uint32_t* occ0, const uint32_t* occ1, int words, int dense_steps, int dhalves,
+                       bool is_dense) {
     dense = is_dense;
     dense_left = dense_steps;
     dense_i = 0;
-    if (!dense) it.init(occ, words);
+    dense_halves = dhalves;
+    if (!dense) it.init(occ0, occ1, words);
   }
-  __device__ __forceinline__ int next() {
-    if (dense) return dense_left-- > 0 ? dense_i++ : -1;
-    return it.next();
+  __device__ __forceinline__ int next(int& halves) {
+    if (dense) {
+      halves = dense_halves;
+      return dense_left-- > 0 ? dense_i++ : -1;
+    }
+    return it.next(halves);
   }
 };
 
@@ -149,29 +170,30 @@ struct StepIter {
 // reduction, SBO = 512 B along M/N); the dense 16-bit operands come by TMA
 // in swizzled layouts.  The modes differ only in the producers, the
 // descriptors and the epilogue.
-template <typename BT, int MODE, int kStages>
+template <typename BT, int MODE>
 __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __grid_constant__ CUtensorMap mapA,
                                                           const __grid_constant__ CUtensorMap mapB) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
-  TcSmem<kStages>& sm = *reinterpret_cast<TcSmem<kStages>*>(
+  TcSmem& sm = *reinterpret_cast<TcSmem*>(
       smem_raw + ((kSmemAlign - (ptx::smem_addr(smem_raw) & (kSmemAlign - 1))) & (kSmemAlign - 1)));
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int64_t row0 = (int64_t)blockIdx.x * kTcM;  // output rows: M (fwd, sddmm) or K (trans)
-  const int64_t col0 = (int64_t)blockIdx.y * kTcN;  // output columns: N (fwd, trans) or K (sddmm)
+  const int64_t row0 = (int64_t)blockIdx.x * kCtaM;  // output rows: M (fwd, sddmm) or K (trans)
+  const int64_t col0 = (int64_t)blockIdx.y * kTcN;   // output columns: N (fwd, trans) or K (sddmm)
   const int64_t out_rows = MODE == kTrans ? a.K : a.M;
   const int64_t out_cols = MODE == kSddmm ? a.K : a.N;
   const uint32_t one = std::is_same<BT, __nv_bfloat16>::value ? 0x3f80u : 0x3c00u;
 
   if (tid == 0) {
     for (int s = 0; s < kStages; s++) {
-      ptx::mbar_init(&sm.full[s], kProducers + 1);  // producers + the TMA transaction arrival
+      // one arrival per producer warp + the TMA warp's (SDDMM: TMA only)
+      ptx::mbar_init(&sm.full[s], MODE == kSddmm ? 1 : kProducerWarps + 1);
       ptx::mbar_init(&sm.empty[s], 1);
     }
     ptx::mbar_init(&sm.done, 1);
     sm.abort = 0;
     ptx::fence_mbar_init();
   }
-  if (warp == 4) {
+  if (warp == kMmaWarp) {
     ptx::tmem_alloc(&sm.tmem_addr, kTmemCols);
     ptx::tmem_relinquish();
   }
@@ -179,7 +201,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
   int any = 1;
   if (MODE == kSddmm) {
     uint32_t acc = 0;
-    if (warp < 4 && row0 + tid < a.M) {
+    if (warp < kProducerWarps && row0 + tid < a.M) {
       const uint32_t* arow = a.A + (row0 + tid) * a.Kw;
       for (int64_t w = col0 / 32; w < min(a.Kw, (col0 + kTcN) / 32); w++) acc |= __ldg(arow + w);
     }
@@ -189,40 +211,101 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
   __syncthreads();
   ptx::tc_fence_after_sync();
   const uint32_t tmem = sm.tmem_addr;
-  const int dense_steps = any ? (int)((a.N + kTcK - 1) / kTcK) : 0;
-  const uint32_t* block_occ = a.occ + (int64_t)blockIdx.x * a.occ_words;
-  int ntiles = 0;
+  // SDDMM steps are whole stages of kSdK columns of N
+  const int dense_steps = any ? (int)((a.N + kSdK - 1) / kSdK) : 0;
+  const int dense_halves = row0 + kTcM < out_rows ? 3 : 1;
+  const int nblk = (int)((out_rows + kTcM - 1) / kTcM);  // 128-row occupancy blocks
+  const uint32_t* occ0 = MODE == kSddmm ? nullptr : a.occ + (int64_t)blockIdx.x * kHalves * a.occ_words;
+  const uint32_t* occ1 = (MODE != kSddmm && (int)blockIdx.x * kHalves + 1 < nblk) ? occ0 + a.occ_words : nullptr;
+  int seen = 0;  // halves that received at least one product (producer warps)
+  // Stage i holds tiles 2i and 2i+1 of the occupied-tile sequence (fwd /
+  // trans), or N columns [64i, 64i+64) (SDDMM).
 
-  if (warp < 4) {
-    // ---------------- producers ----------------
-    // Operands that are dense 16-bit tiles come by TMA (warp 0 issues the
-    // boxes and the stage's transaction count); the bit tiles of A are
-    // expanded by all 128 producers from words loaded two tiles ahead.
+  if (warp < kProducerWarps) {
+    // ---------------- A producers ----------------
+    // Each thread expands one word per tile (two per stage), loaded kLook
+    // tiles ahead; the warp arrives once per stage after its lanes' writes
+    // are fenced.  Lane 0 waits for the slot on behalf of the warp.
     StepIter it;
-    it.init(block_occ, a.occ_words, dense_steps, MODE == kSddmm);
-    auto load_word = [&](int t) -> uint32_t {
-      if (t < 0 || MODE == kSddmm) return 0u;
-      if (MODE == kFwd) {
-        const int64_t arow = row0 + tid;
-        return arow < a.M ? __ldg(a.A + arow * a.Kw + t) : 0u;
+    it.init(occ0, occ1, a.occ_words, dense_steps, dense_halves, MODE == kSddmm);
+    if (MODE == kSddmm) {
+      int h = 0;
+      while (it.next(h) >= 0) seen |= h;
+    } else {
+      auto load_word = [&](int t) -> uint32_t {
+        if (t < 0) return 0u;
+        if (MODE == kFwd) {
+          const int64_t arow = row0 + tid;
+          return arow < a.M ? __ldg(a.A + arow * a.Kw + t) : 0u;
+        }
+        const int64_t arow = (int64_t)t * kTcK + (tid & 31);
+        const int64_t wcol = row0 / 32 + (tid >> 5);
+        return (arow < a.M && wcol < a.Kw) ? __ldg(a.A + arow * a.Kw + wcol) : 0u;
+      };
+      // tq[0] is the next tile to expand, tq[1..kLook] the ones after it;
+      // wq[j] holds the A word of tq[j]
+      int tq[kLook + 1];
+      uint32_t wq[kLook];
+#pragma unroll
+      for (int j = 0; j <= kLook; j++) {
+        int h = 0;
+        tq[j] = (j == 0 || tq[j - 1] >= 0) ? it.next(h) : -1;
+        if (tq[j] >= 0) seen |= h;
       }
-      const int64_t arow = (int64_t)t * kTcK + (tid & 31);
-      const int64_t wcol = row0 / 32 + (tid >> 5);
-      return (arow < a.M && wcol < a.Kw) ? __ldg(a.A + arow * a.Kw + wcol) : 0u;
-    };
-    // tq[0] is the current tile, tq[1..kLook] the next ones; wq[j] holds the
-    // A word of tq[j] (loads issued kLook tiles before use)
-    int tq[kLook + 1];
-    uint32_t wq[kLook];
 #pragma unroll
-    for (int j = 0; j <= kLook; j++) tq[j] = (j == 0 || tq[j - 1] >= 0) ? it.next() : -1;
+      for (int j = 0; j < kLook; j++) wq[j] = load_word(tq[j]);
+      for (int i = 0; tq[0] >= 0; i++) {
+        const int s = i % kStages;
+        int go = 1;
+        if (lane == 0) {
+          if (i >= kStages && !ptx::mbar_wait(&sm.empty[s], ((i / kStages) - 1) & 1)) {
+            atomicCAS(&g_tc_error, 0, 3);
+            sm.abort = 1;
+          }
+          go = !*(volatile int*)&sm.abort;
+        }
+        if (!__shfl_sync(kFull, go, 0)) break;
 #pragma unroll
-    for (int j = 0; j < kLook; j++) wq[j] = load_word(tq[j]);
-    int i = 0;
-    for (; tq[0] >= 0; i++) {
-      const int t0 = tq[0];
-      const uint32_t w0 = wq[0];
-      const uint32_t wnew = load_word(tq[kLook]);
+        for (int u = 0; u < kTilesPerStage; u++) {
+          if (tq[0] < 0) break;
+          const uint32_t w0 = wq[0];
+          const uint32_t wnew = load_word(tq[kLook]);
+          uint8_t* at = sm.a[s] + u * kATile;
+          if (MODE == kFwd) {
+            // row tid of the tile: half tid/128 at 8 KB, then core matrices
+            uint8_t* as = at + (tid >> 3) * kSbo + (tid & 7) * 16;
+#pragma unroll
+            for (int c = 0; c < 4; c++)
+              *reinterpret_cast<uint4*>(as + c * kLbo) = expand8((w0 >> (8 * c)) & 0xffu, one);
+          } else {
+            // A row j of the tile, word wk of the block: output rows wk*32 + 8c ..
+            const int j = tid & 31, wk = tid >> 5;
+            uint8_t* as = at + (j >> 3) * kLbo + (j & 7) * 16;
+#pragma unroll
+            for (int c = 0; c < 4; c++)
+              *reinterpret_cast<uint4*>(as + (wk * 4 + c) * kSbo) = expand8((w0 >> (8 * c)) & 0xffu, one);
+          }
+#pragma unroll
+          for (int j = 0; j < kLook - 1; j++) wq[j] = wq[j + 1];
+          wq[kLook - 1] = wnew;
+#pragma unroll
+          for (int j = 0; j < kLook; j++) tq[j] = tq[j + 1];
+          int h = 0;
+          tq[kLook] = tq[kLook] >= 0 ? it.next(h) : -1;
+          if (tq[kLook] >= 0) seen |= h;
+        }
+        ptx::fence_proxy_async_smem();
+        __syncwarp();
+        if (lane == 0) ptx::mbar_arrive(&sm.full[s]);
+      }
+    }
+  } else if (warp == kTmaWarp && lane == 0) {
+    // ---------------- TMA issuer ----------------
+    StepIter it;
+    it.init(occ0, occ1, a.occ_words, dense_steps, dense_halves, MODE == kSddmm);
+    int h = 0;
+    int t = it.next(h);
+    for (int i = 0; t >= 0; i++) {
       const int s = i % kStages;
       if (i >= kStages && !ptx::mbar_wait(&sm.empty[s], ((i / kStages) - 1) & 1)) {
         atomicCAS(&g_tc_error, 0, 3);
@@ -230,48 +313,41 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
         break;
       }
       if (*(volatile int*)&sm.abort) break;
-      if (warp == 0) {
-        if (lane == 0) ptx::mbar_arrive_expect_tx(&sm.full[s], MODE == kSddmm ? kAStage + kBStage : kBStage);
-        __syncwarp();
-        if (MODE == kSddmm) {
-          // G rows row0.. and X rows col0.., columns t0*32..: one box each
-          if (lane == 0) ptx::tma_load_2d(sm.a[s], &mapA, t0 * kTcK, (int)row0, &sm.full[s]);
-          else if (lane == 1) ptx::tma_load_2d(sm.b[s], &mapB, t0 * kTcK, (int)col0, &sm.full[s]);
-        } else if (lane < kTcN / kBoxCols) {
-          // B (fwd) / G (trans): reduction rows t0*32.., columns col0 + 64*lane
-          ptx::tma_load_2d(sm.b[s] + lane * kBox, &mapB, (int)col0 + lane * kBoxCols, t0 * kTcK, &sm.full[s]);
+      if (MODE == kSddmm) {
+        // G rows row0.. and X rows col0.. (256 each), N columns t*64..
+        ptx::mbar_arrive_expect_tx(&sm.full[s], 2 * kStageBytes);
+        ptx::tma_load_2d(sm.a[s], &mapA, t * kSdK, (int)row0, &sm.full[s]);
+        ptx::tma_load_2d(sm.b[s], &mapB, t * kSdK, (int)col0, &sm.full[s]);
+        t = it.next(h);
+      } else {
+        // B (fwd) / G (trans) rows t*32.. of each of the stage's tiles,
+        // columns col0 + 64*j
+        const int t1 = it.next(h);
+        ptx::mbar_arrive_expect_tx(&sm.full[s], (t1 >= 0 ? 2 : 1) * kBTile);
+#pragma unroll
+        for (int j = 0; j < kTcN / kBoxCols; j++)
+          ptx::tma_load_2d(sm.b[s] + j * kBox, &mapB, (int)col0 + j * kBoxCols, t * kTcK, &sm.full[s]);
+        if (t1 >= 0) {
+#pragma unroll
+          for (int j = 0; j < kTcN / kBoxCols; j++)
+            ptx::tma_load_2d(sm.b[s] + kBTile + j * kBox, &mapB, (int)col0 + j * kBoxCols, t1 * kTcK, &sm.full[s]);
         }
+        t = t1 >= 0 ? it.next(h) : -1;
       }
-      if (MODE == kFwd) {
-        uint8_t* as = sm.a[s] + (tid >> 3) * kSbo + (tid & 7) * 16;
-#pragma unroll
-        for (int c = 0; c < 4; c++) *reinterpret_cast<uint4*>(as + c * kLbo) = expand8((w0 >> (8 * c)) & 0xffu, one);
-      } else if (MODE == kTrans) {
-        const int j = tid & 31, wk = tid >> 5;
-        uint8_t* as = sm.a[s] + (j >> 3) * kLbo + (j & 7) * 16;
-#pragma unroll
-        for (int c = 0; c < 4; c++)
-          *reinterpret_cast<uint4*>(as + (wk * 4 + c) * kSbo) = expand8((w0 >> (8 * c)) & 0xffu, one);
-      }
-      ptx::fence_proxy_async_smem();
-      ptx::mbar_arrive(&sm.full[s]);
-#pragma unroll
-      for (int j = 0; j < kLook - 1; j++) wq[j] = wq[j + 1];
-      wq[kLook - 1] = wnew;
-#pragma unroll
-      for (int j = 0; j < kLook; j++) tq[j] = tq[j + 1];
-      tq[kLook] = tq[kLook] >= 0 ? it.next() : -1;
     }
-    ntiles = i;
-  } else if (lane == 0) {
+  } else if (warp == kMmaWarp && lane == 0) {
     // ---------------- MMA issuer ----------------
     const uint32_t ab = std::is_same<BT, __nv_bfloat16>::value ? 1u : 0u;
     const uint32_t idesc = idesc_f16(ab, MODE == kTrans ? 1u : 0u, MODE == kSddmm ? 0u : 1u);
     StepIter it;
-    it.init(block_occ, a.occ_words, dense_steps, MODE == kSddmm);
-    int i = 0;
-    for (int t = it.next(); t >= 0; t = it.next(), i++) {
+    it.init(occ0, occ1, a.occ_words, dense_steps, dense_halves, MODE == kSddmm);
+    int i = 0, started = 0;
+    int hv[kTilesPerStage];
+    int t = it.next(hv[0]);
+    for (; t >= 0; i++) {
       const int s = i % kStages;
+      int nt = 1;
+      if (MODE != kSddmm) nt = it.next(hv[1]) >= 0 ? 2 : 1;
       if (!ptx::mbar_wait(&sm.full[s], (i / kStages) & 1)) {
         atomicCAS(&g_tc_error, 0, 3);
         sm.abort = 1;
@@ -279,49 +355,73 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
       }
       if (*(volatile int*)&sm.abort) break;
       ptx::tc_fence_after_sync();
+      if (MODE == kSddmm) {
 #pragma unroll
-      for (int j = 0; j < 2; j++) {
-        uint64_t ad, bd;
-        if (MODE == kSddmm) {  // both K-major, 64-byte swizzle; K half j starts 32 B in
-          ad = ptx::smem_desc_swizzle(sm.a[s] + j * 32, 16, kSdSbo, kLayoutSw64);
-          bd = ptx::smem_desc_swizzle(sm.b[s] + j * 32, 16, kSdSbo, kLayoutSw64);
-        } else {  // A: core matrices; B: 128-byte swizzle, K half j = two 8-row groups on
-          ad = ptx::smem_desc_noswizzle(sm.a[s] + j * 2 * kLbo, kLbo, kSbo);
-          bd = ptx::smem_desc_swizzle(sm.b[s] + j * 2 * 1024, kBox, 1024, kLayoutSw128);
+        for (int h = 0; h < kHalves; h++) {
+          if (!((hv[0] >> h) & 1)) continue;
+#pragma unroll
+          for (int j = 0; j < kSdK / 16; j++) {
+            // both K-major, 128-byte swizzle; K step j starts 32 B into the rows
+            const uint64_t ad = ptx::smem_desc_swizzle(sm.a[s] + h * (kTcM * 128) + j * 32, 16, kSdSbo, kLayoutSw128);
+            const uint64_t bd = ptx::smem_desc_swizzle(sm.b[s] + j * 32, 16, kSdSbo, kLayoutSw128);
+            ptx::tc_mma_f16(tmem + (uint32_t)(h * kTcN), ad, bd, idesc, ((started >> h) & 1) || (j > 0));
+          }
+          started |= 1 << h;
         }
-        ptx::tc_mma_f16(tmem, ad, bd, idesc, (i > 0) || (j > 0));
+      } else {
+#pragma unroll
+        for (int u = 0; u < kTilesPerStage; u++) {
+          if (u >= nt) break;
+#pragma unroll
+          for (int h = 0; h < kHalves; h++) {
+            if (!((hv[u] >> h) & 1)) continue;
+#pragma unroll
+            for (int j = 0; j < 2; j++) {
+              // A: core matrices; B: 128-byte swizzle, K half j = two 8-row groups on
+              const uint64_t ad =
+                  ptx::smem_desc_noswizzle(sm.a[s] + u * kATile + h * kAHalf + j * 2 * kLbo, kLbo, kSbo);
+              const uint64_t bd = ptx::smem_desc_swizzle(sm.b[s] + u * kBTile + j * 2 * 1024, kBox, 1024, kLayoutSw128);
+              ptx::tc_mma_f16(tmem + (uint32_t)(h * kTcN), ad, bd, idesc, ((started >> h) & 1) || (j > 0));
+            }
+            started |= 1 << h;
+          }
+        }
       }
       ptx::tc_commit(&sm.empty[s]);
+      t = (MODE == kSddmm || nt == 2) ? it.next(hv[0]) : -1;
     }
     if (i > 0) ptx::tc_commit(&sm.done);
     else ptx::mbar_arrive(&sm.done);
   }
 
-  // ---------------- epilogue (warps 0-3) ----------------
-  if (warp < 4) {
-    const bool have = ntiles > 0;
+  // ---------------- epilogue (producer warps) ----------------
+  // Warp w reads TMEM lanes 32*(w%4).. of accumulator w/4 (a warp may only
+  // touch its own quarter of the lanes); a thread owns one output row.
+  if (warp < kProducerWarps) {
+    const int h = warp >> 2, q = warp & 3;
+    const bool have = (seen >> h) & 1;
     bool ok = ptx::mbar_wait(&sm.done, 0);
     if (!ok) {
       atomicCAS(&g_tc_error, 0, 3);
       sm.abort = 1;
     }
     ptx::tc_fence_after_sync();
-    const int64_t row = row0 + warp * 32 + lane;
+    const int64_t row = row0 + h * kTcM + q * 32 + lane;
     float* crow = a.C + row * a.ldc + col0;
     const bool live = row < out_rows && ok && !*(volatile int*)&sm.abort;
     const uint32_t* arow = a.A + row * a.Kw;
+    const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * kTcN);
     for (int c8 = 0; c8 < kTcN / 8; c8 += 4) {
       uint32_t r[4][8];
       if (have && ok) {
 #pragma unroll
-        for (int u = 0; u < 4; u++)
-          ptx::tmem_ld_32x32b_x8(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)((c8 + u) * 8), r[u]);
+        for (int u = 0; u < 4; u++) ptx::tmem_ld_32x32b_x8(tbase + (uint32_t)((c8 + u) * 8), r[u]);
         ptx::tmem_wait_ld();
       } else {
 #pragma unroll
         for (int u = 0; u < 4; u++)
 #pragma unroll
-          for (int q = 0; q < 8; q++) r[u][q] = 0u;
+          for (int v = 0; v < 8; v++) r[u][v] = 0u;
       }
       if (!live) continue;
 #pragma unroll
@@ -331,8 +431,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
         if (MODE == kSddmm) {  // keep the set bits of A's row only
           const uint32_t bits = (__ldg(arow + (col0 + col) / 32) >> ((col0 + col) & 31)) & 0xffu;
 #pragma unroll
-          for (int q = 0; q < 8; q++)
-            if (!((bits >> q) & 1u)) r[u][q] = 0u;
+          for (int v = 0; v < 8; v++)
+            if (!((bits >> v) & 1u)) r[u][v] = 0u;
         }
         *reinterpret_cast<float4*>(crow + col) = make_float4(
             __uint_as_float(r[u][0]), __uint_as_float(r[u][1]), __uint_as_float(r[u][2]), __uint_as_float(r[u][3]));
@@ -343,7 +443,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
   }
   ptx::tc_fence_before_sync();
   __syncthreads();
-  if (warp == 4) {
+  if (warp == kMmaWarp) {
     ptx::tc_fence_after_sync();
     ptx::tmem_dealloc(tmem, kTmemCols);
   }
@@ -455,40 +555,21 @@ int make_map(CUtensorMap* m, const void* base, int dt, int64_t rows, int64_t col
   return r == CUDA_SUCCESS ? BSP_OK : BSP_ERR_ALIGNMENT;
 }
 
-template <typename BT, int MODE, int S>
-int launch_stages(const TcArgs& a, const CUtensorMap& ma, const CUtensorMap& mb, dim3 grid, cudaStream_t s) {
-  const size_t smem = sizeof(TcSmem<S>) + kSmemAlign;
+static_assert(sizeof(TcSmem) + kSmemAlign <= 232448, "stage ring exceeds the shared memory of a CTA");
+
+template <typename BT, int MODE>
+int launch_mode(const TcArgs& a, const CUtensorMap& ma, const CUtensorMap& mb, dim3 grid, cudaStream_t s) {
+  const size_t smem = sizeof(TcSmem) + kSmemAlign;
   static bool configured[64] = {};
   int dev = 0;
   BSP_CUDA(cudaGetDevice(&dev));
   if (dev < 64 && !configured[dev]) {
-    BSP_CUDA(cudaFuncSetAttribute(k_spmm_tc<BT, MODE, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    BSP_CUDA(cudaFuncSetAttribute(k_spmm_tc<BT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     configured[dev] = true;
   }
-  k_spmm_tc<BT, MODE, S><<<grid, kTcThreads, smem, s>>>(a, ma, mb);
+  k_spmm_tc<BT, MODE><<<grid, kTcThreads, smem, s>>>(a, ma, mb);
   BSP_LAUNCHED();
   return BSP_OK;
-}
-
-// Stage ring depth: 4 stages (two CTAs per SM) or 6 / 8 (one CTA per SM);
-// BSP_TC_STAGES selects it for tuning.
-int tc_stages() {
-  static int v = 0;
-  if (!v) {
-    const char* e = getenv("BSP_TC_STAGES");
-    v = e ? atoi(e) : 4;
-    if (v != 4 && v != 6 && v != 8) v = 4;
-  }
-  return v;
-}
-
-template <typename BT, int MODE>
-int launch_mode(const TcArgs& a, const CUtensorMap& ma, const CUtensorMap& mb, dim3 grid, cudaStream_t s) {
-  switch (tc_stages()) {
-    case 6: return launch_stages<BT, MODE, 6>(a, ma, mb, grid, s);
-    case 8: return launch_stages<BT, MODE, 8>(a, ma, mb, grid, s);
-    default: return launch_stages<BT, MODE, 4>(a, ma, mb, grid, s);
-  }
 }
 
 template <int MODE>
@@ -496,14 +577,14 @@ int launch_tc(const TcArgs& a, cudaStream_t s) {
   const int64_t rows = MODE == kTrans ? a.K : a.M;
   const int64_t cols = MODE == kSddmm ? a.K : a.N;
   if (rows == 0 || cols == 0) return BSP_OK;
-  const dim3 grid((unsigned)ceil_div(rows, kTcM), (unsigned)ceil_div(cols, kTcN));
-  if (ceil_div(cols, kTcN) > 65535 || ceil_div(rows, kTcM) > 0x7fffffff) return BSP_ERR_CAPACITY;
+  const dim3 grid((unsigned)ceil_div(rows, kCtaM), (unsigned)ceil_div(cols, kTcN));
+  if (ceil_div(cols, kTcN) > 65535 || ceil_div(rows, kCtaM) > 0x7fffffff) return BSP_ERR_CAPACITY;
   if (a.N > INT32_MAX || a.M > INT32_MAX || a.K > INT32_MAX) return BSP_ERR_CAPACITY;
   CUtensorMap ma, mb;
   memset(&ma, 0, sizeof(ma));
   if (MODE == kSddmm) {
-    BSP_TRY(make_map(&ma, a.G, a.bdt, a.M, a.N, a.ldg, kTcK, kTcM, CU_TENSOR_MAP_SWIZZLE_64B));  // G [M][N]
-    BSP_TRY(make_map(&mb, a.B, a.bdt, a.K, a.N, a.ldb, kTcK, kTcN, CU_TENSOR_MAP_SWIZZLE_64B));  // X [K][N]
+    BSP_TRY(make_map(&ma, a.G, a.bdt, a.M, a.N, a.ldg, kSdK, kCtaM, CU_TENSOR_MAP_SWIZZLE_128B));  // G [M][N]
+    BSP_TRY(make_map(&mb, a.B, a.bdt, a.K, a.N, a.ldb, kSdK, kTcN, CU_TENSOR_MAP_SWIZZLE_128B));   // X [K][N]
   } else {
     // B [K][N] (fwd) or G [M][N] (trans), 64 columns x 32 reduction rows per box
     BSP_TRY(make_map(&mb, a.B, a.bdt, MODE == kFwd ? a.K : a.M, a.N, a.ldb, kBoxCols, kTcK,
