@@ -219,6 +219,7 @@ static int64_t proto_ldp(int64_t N) { return (N + 7) / 8 * 8; }
 // occupied (128 x 32) tiles at ~1.2 PFLOP/s against the B-row gathers of the
 // CUDA-core schedule at ~8 TB/s (rates measured on GB300).
 static bool use_tensor_cores(const bsp_plan* plan, int64_t N, int esize) {
+  if (plan->K > tc_max_reduction()) return false;
   const char* e = getenv("BSP_TC");
   if (e) return e[0] == '1';
   const double tc = (double)plan->occ_tiles * 128.0 * 32.0 * (double)N * 2.0 / 1.2e15;
@@ -357,7 +358,7 @@ int bsp_spmm_t(const uint32_t* A_words, int64_t M, int64_t K, const void* G, int
   }
   const int vcols = g_dtype == BSP_F32 ? 4 : 8;
   const bool vec = layout16(G, ldg, esz, N, vcols) && layout16(dX, lddx, 4, N, 4);
-  if (plan && vec && g_dtype != BSP_F32) {
+  if (plan && vec && g_dtype != BSP_F32 && M <= tc_max_reduction()) {
     const char* e = getenv("BSP_TC");
     const double tc = (double)plan->occT_tiles * 128.0 * 32.0 * (double)N * 2.0 / 1.2e15;
     const double cc = (double)plan->nnz * (double)N * (double)esz / 8e12;

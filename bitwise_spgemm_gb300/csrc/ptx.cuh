@@ -150,6 +150,13 @@ __device__ __forceinline__ void cp_async_wait_group() {
 // bytes), completing as transaction bytes on `bar`.  `map` is the address of
 // a __grid_constant__ CUtensorMap kernel parameter.  Boxes reaching past the
 // tensor are zero-filled.
+__device__ __forceinline__ void tma_load_2d_u32(uint32_t dst_smem, const void* map, int x, int y, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          dst_smem),
+      "l"(map), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
 __device__ __forceinline__ void tma_load_2d(void* dst_smem, const void* map, int x, int y, uint64_t* bar) {
   asm volatile(
       "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
@@ -160,6 +167,11 @@ __device__ __forceinline__ void tma_load_2d(void* dst_smem, const void* map, int
 
 // Shared-memory matrix descriptor (tcgen05), no swizzle: start address,
 // leading-dimension byte offset, stride byte offset (all >> 4), version 1.
+__device__ __forceinline__ uint64_t smem_desc_noswizzle_u32(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  const uint64_t addr = (uint64_t)(saddr & 0x3ffffu) >> 4;
+  return addr | ((uint64_t)((lbo >> 4) & 0x3fffu) << 16) | ((uint64_t)((sbo >> 4) & 0x3fffu) << 32) |
+         (1ull << 46);
+}
 __device__ __forceinline__ uint64_t smem_desc_noswizzle(const void* p, uint32_t lbo, uint32_t sbo) {
   const uint64_t addr = (uint64_t)(smem_addr(p) & 0x3ffffu) >> 4;
   return addr | ((uint64_t)((lbo >> 4) & 0x3fffu) << 16) | ((uint64_t)((sbo >> 4) & 0x3fffu) << 32) |

@@ -44,6 +44,9 @@ int bulk_device_error(int* out, bool clear);
 // K tiles per 128-row block ([ceil(M/128)][tc_occupancy_words(K)]), then the
 // tcgen05 kernel over the occupied tiles.
 int tc_occupancy_words(int64_t K);
+// Longest reduction (K forward, M transposed) the tensor-core kernels take:
+// a CTA lists its occupied 32-column tiles in shared memory.
+int64_t tc_max_reduction();
 int tc_occupancy_t_words(int64_t M);
 int launch_tile_occupancy(const uint32_t* A, int64_t M, int64_t K, uint32_t* occ,
                           unsigned long long* count, cudaStream_t s);

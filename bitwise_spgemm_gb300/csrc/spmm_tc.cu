@@ -49,17 +49,23 @@ constexpr int kCtaM = kTcM * kHalves;     // ... 256 output rows, sharing every 
 constexpr int kTcN = 256;
 constexpr int kTcK = 32;                  // one packed word of A per row and K tile
 constexpr int kTilesPerStage = 2;         // a stage carries two occupied K tiles
-constexpr int kLook = 8;                  // A words are loaded this many K tiles ahead
 constexpr int kATile = kCtaM * kTcK * 2;  // 16 KB: both halves of one K tile
 constexpr int kAHalf = kTcM * kTcK * 2;   // 8 KB
 constexpr int kBTile = kTcK * kTcN * 2;   // 16 KB
 constexpr int kStageBytes = kTilesPerStage * kATile;  // per operand: 32 KB
 constexpr int kStages = 3;
-constexpr int kProducers = kCtaM;         // one producer thread per row of the CTA tile
+// Producers: one group of 256 threads (one per row of the CTA tile) per tile
+// of the stage, so a warp expands one tile per stage.
+constexpr int kGroupThreads = kCtaM;
+constexpr int kProducers = kGroupThreads * kTilesPerStage;
 constexpr int kProducerWarps = kProducers / 32;
 constexpr int kTmaWarp = kProducerWarps;      // issues the TMA boxes
 constexpr int kMmaWarp = kProducerWarps + 1;  // allocates TMEM, issues the MMAs
 constexpr int kTcThreads = kProducers + 64;
+constexpr int kWordAhead = 4;                 // A words are loaded this many stages ahead
+// Occupied K tiles of the CTA, listed once in shared memory: tile index in
+// bits 0-27, which 128-row halves have bits in bits 28-29.
+constexpr int kListMax = 4096;
 constexpr uint32_t kTmemCols = 512;       // two 128x256 FP32 accumulators
 using tc::kLbo;
 using tc::kSbo;
@@ -82,6 +88,8 @@ constexpr size_t kSmemAlign = 1024;
 struct __align__(1024) TcSmem {
   uint8_t a[kStages][kStageBytes];
   uint8_t b[kStages][kStageBytes];
+  int list[kListMax];
+  int nlist, seen;
   uint64_t full[kStages];   // producer warps + the TMA transaction arrival
   uint64_t empty[kStages];  // tcgen05.commit of the stage's MMAs
   uint64_t done;
@@ -108,58 +116,6 @@ struct TcArgs {
   int bdt;
 };
 
-// Occupied K tiles of the CTA's two 128-row blocks (forward: K tiles; trans:
-// row tiles of A), ascending over the union; `halves` tells which of the two
-// blocks have bits in the returned tile (bit 0 = first block).
-struct TileIter {
-  const uint32_t* o0;
-  const uint32_t* o1;  // null when the second block lies past the end
-  int ow, nw;
-  uint32_t bits, b0, b1;
-  __device__ void init(const uint32_t* p0, const uint32_t* p1, int n) {
-    o0 = p0;
-    o1 = p1;
-    nw = n;
-    ow = -1;
-    bits = b0 = b1 = 0;
-  }
-  __device__ __forceinline__ int next(int& halves) {
-    while (bits == 0) {
-      if (++ow >= nw) return -1;
-      b0 = __ldg(o0 + ow);
-      b1 = o1 ? __ldg(o1 + ow) : 0u;
-      bits = b0 | b1;
-    }
-    const int b = __ffs(bits) - 1;
-    bits &= bits - 1;
-    halves = (int)(((b0 >> b) & 1u) | (((b1 >> b) & 1u) << 1));
-    return ow * 32 + b;
-  }
-};
-
-// Steps of the reduction: occupied tiles (forward / trans) or every
-// 32-column step of N (SDDMM, both halves unless the second is past the end).
-struct StepIter {
-  TileIter it;
-  int dense_left, dense_i, dense_halves;
-  bool dense;
-  __device__ void init(const uint32_t* occ0, const uint32_t* occ1, int words, int dense_steps, int dhalves,
-                       bool is_dense) {
-    dense = is_dense;
-    dense_left = dense_steps;
-    dense_i = 0;
-    dense_halves = dhalves;
-    if (!dense) it.init(occ0, occ1, words);
-  }
-  __device__ __forceinline__ int next(int& halves) {
-    if (dense) {
-      halves = dense_halves;
-      return dense_left-- > 0 ? dense_i++ : -1;
-    }
-    return it.next(halves);
-  }
-};
-
 // One kernel, three products (MODE):
 //   kFwd   C[M,N]  = A · B        A bits K-major from A's words, B MN-major
 //   kTrans C[K,N]  = Aᵀ · G       Aᵀ MN-major built from A's row words (no
@@ -182,6 +138,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
   const int64_t out_rows = MODE == kTrans ? a.K : a.M;
   const int64_t out_cols = MODE == kSddmm ? a.K : a.N;
   const uint32_t one = std::is_same<BT, __nv_bfloat16>::value ? 0x3f80u : 0x3c00u;
+  const int dense_halves = row0 + kTcM < out_rows ? 3 : 1;
 
   if (tid == 0) {
     for (int s = 0; s < kStages; s++) {
@@ -197,65 +154,93 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
     ptx::tmem_alloc(&sm.tmem_addr, kTmemCols);
     ptx::tmem_relinquish();
   }
+  if (MODE != kSddmm && warp == 0) {
+    // List the occupied K tiles of the two 128-row blocks (ascending), with
+    // the halves that have bits in each; the launcher guarantees that the
+    // list fits (at most kListMax reduction tiles).
+    const int nblk = (int)((out_rows + kTcM - 1) / kTcM);
+    const uint32_t* occ0 = a.occ + (int64_t)blockIdx.x * kHalves * a.occ_words;
+    const bool has1 = (int)blockIdx.x * kHalves + 1 < nblk;
+    int n = 0;
+    uint32_t any0 = 0, any1 = 0;
+    for (int ow0 = 0; ow0 < a.occ_words; ow0 += 32) {
+      const int ow = ow0 + lane;
+      const uint32_t b0 = ow < a.occ_words ? __ldg(occ0 + ow) : 0u;
+      const uint32_t b1 = (has1 && ow < a.occ_words) ? __ldg(occ0 + a.occ_words + ow) : 0u;
+      any0 |= b0;
+      any1 |= b1;
+      uint32_t bits = b0 | b1;
+      const int c = __popc(bits);
+      int incl = c;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const int y = __shfl_up_sync(kFull, incl, d);
+        if (lane >= d) incl += y;
+      }
+      int pos = n + incl - c;
+      while (bits) {
+        const int b = __ffs(bits) - 1;
+        bits &= bits - 1;
+        if (pos < kListMax)
+          sm.list[pos] = (ow * 32 + b) | (int)((((b0 >> b) & 1u) | (((b1 >> b) & 1u) << 1)) << 28);
+        pos++;
+      }
+      n += __shfl_sync(kFull, incl, 31);
+    }
+    const int seen = (__any_sync(kFull, any0 != 0u) ? 1 : 0) | (__any_sync(kFull, any1 != 0u) ? 2 : 0);
+    if (lane == 0) {
+      sm.nlist = min(n, kListMax);
+      sm.seen = seen;
+    }
+  }
   // SDDMM: a block of A without set bits needs no product at all
-  int any = 1;
   if (MODE == kSddmm) {
     uint32_t acc = 0;
-    if (warp < kProducerWarps && row0 + tid < a.M) {
+    if (tid < kCtaM && row0 + tid < a.M) {
       const uint32_t* arow = a.A + (row0 + tid) * a.Kw;
       for (int64_t w = col0 / 32; w < min(a.Kw, (col0 + kTcN) / 32); w++) acc |= __ldg(arow + w);
     }
-    any = __syncthreads_or(acc != 0u);
+    const int any = __syncthreads_or(acc != 0u);
+    if (tid == 0) {
+      sm.nlist = any ? (int)((a.N + kSdK - 1) / kSdK) : 0;  // steps of kSdK columns of N
+      sm.seen = any ? dense_halves : 0;
+    }
   }
   ptx::tc_fence_before_sync();
   __syncthreads();
   ptx::tc_fence_after_sync();
   const uint32_t tmem = sm.tmem_addr;
-  // SDDMM steps are whole stages of kSdK columns of N
-  const int dense_steps = any ? (int)((a.N + kSdK - 1) / kSdK) : 0;
-  const int dense_halves = row0 + kTcM < out_rows ? 3 : 1;
-  const int nblk = (int)((out_rows + kTcM - 1) / kTcM);  // 128-row occupancy blocks
-  const uint32_t* occ0 = MODE == kSddmm ? nullptr : a.occ + (int64_t)blockIdx.x * kHalves * a.occ_words;
-  const uint32_t* occ1 = (MODE != kSddmm && (int)blockIdx.x * kHalves + 1 < nblk) ? occ0 + a.occ_words : nullptr;
-  int seen = 0;  // halves that received at least one product (producer warps)
-  // Stage i holds tiles 2i and 2i+1 of the occupied-tile sequence (fwd /
-  // trans), or N columns [64i, 64i+64) (SDDMM).
+  const int n = sm.nlist;
+  // stage i: list entries 2i and 2i+1 (fwd / trans) or N columns [64i, 64i+64) (SDDMM)
+  const int nstages = MODE == kSddmm ? n : (n + kTilesPerStage - 1) / kTilesPerStage;
 
   if (warp < kProducerWarps) {
-    // ---------------- A producers ----------------
-    // Each thread expands one word per tile (two per stage), loaded kLook
-    // tiles ahead; the warp arrives once per stage after its lanes' writes
-    // are fenced.  Lane 0 waits for the slot on behalf of the warp.
-    StepIter it;
-    it.init(occ0, occ1, a.occ_words, dense_steps, dense_halves, MODE == kSddmm);
-    if (MODE == kSddmm) {
-      int h = 0;
-      while (it.next(h) >= 0) seen |= h;
-    } else {
-      auto load_word = [&](int t) -> uint32_t {
-        if (t < 0) return 0u;
+    // ---------------- A producers (fwd / trans) ----------------
+    // Group u (warps 8u..8u+7) expands tile u of every stage, one row (fwd)
+    // or one (A row, word) pair (trans) per thread, from words loaded
+    // kWordAhead stages ahead; each warp arrives once per stage after its
+    // lanes' writes are fenced.  Lane 0 waits for the slot for the warp.
+    if (MODE != kSddmm) {
+      const int u = warp / (kGroupThreads / 32);
+      const int r = tid % kGroupThreads;
+      auto load_word = [&](int k) -> uint32_t {
+        if (k >= n) return 0u;
+        const int t = sm.list[k] & 0x0fffffff;
         if (MODE == kFwd) {
-          const int64_t arow = row0 + tid;
+          const int64_t arow = row0 + r;
           return arow < a.M ? __ldg(a.A + arow * a.Kw + t) : 0u;
         }
-        const int64_t arow = (int64_t)t * kTcK + (tid & 31);
-        const int64_t wcol = row0 / 32 + (tid >> 5);
+        const int64_t arow = (int64_t)t * kTcK + (r & 31);
+        const int64_t wcol = row0 / 32 + (r >> 5);
         return (arow < a.M && wcol < a.Kw) ? __ldg(a.A + arow * a.Kw + wcol) : 0u;
       };
-      // tq[0] is the next tile to expand, tq[1..kLook] the ones after it;
-      // wq[j] holds the A word of tq[j]
-      int tq[kLook + 1];
-      uint32_t wq[kLook];
+      uint32_t wq[kWordAhead];
 #pragma unroll
-      for (int j = 0; j <= kLook; j++) {
-        int h = 0;
-        tq[j] = (j == 0 || tq[j - 1] >= 0) ? it.next(h) : -1;
-        if (tq[j] >= 0) seen |= h;
-      }
-#pragma unroll
-      for (int j = 0; j < kLook; j++) wq[j] = load_word(tq[j]);
-      for (int i = 0; tq[0] >= 0; i++) {
+      for (int j = 0; j < kWordAhead; j++) wq[j] = load_word(kTilesPerStage * j + u);
+      for (int i = 0; i < nstages; i++) {
         const int s = i % kStages;
+        const uint32_t w0 = wq[0];
+        const uint32_t wnew = load_word(kTilesPerStage * (i + kWordAhead) + u);
         int go = 1;
         if (lane == 0) {
           if (i >= kStages && !ptx::mbar_wait(&sm.empty[s], ((i / kStages) - 1) & 1)) {
@@ -265,47 +250,36 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
           go = !*(volatile int*)&sm.abort;
         }
         if (!__shfl_sync(kFull, go, 0)) break;
-#pragma unroll
-        for (int u = 0; u < kTilesPerStage; u++) {
-          if (tq[0] < 0) break;
-          const uint32_t w0 = wq[0];
-          const uint32_t wnew = load_word(tq[kLook]);
+        if (kTilesPerStage * i + u < n) {
           uint8_t* at = sm.a[s] + u * kATile;
           if (MODE == kFwd) {
-            // row tid of the tile: half tid/128 at 8 KB, then core matrices
-            uint8_t* as = at + (tid >> 3) * kSbo + (tid & 7) * 16;
+            // row r of the tile: half r/128 at 8 KB, then core matrices
+            uint8_t* as = at + (r >> 3) * kSbo + (r & 7) * 16;
 #pragma unroll
             for (int c = 0; c < 4; c++)
               *reinterpret_cast<uint4*>(as + c * kLbo) = expand8((w0 >> (8 * c)) & 0xffu, one);
           } else {
             // A row j of the tile, word wk of the block: output rows wk*32 + 8c ..
-            const int j = tid & 31, wk = tid >> 5;
+            const int j = r & 31, wk = r >> 5;
             uint8_t* as = at + (j >> 3) * kLbo + (j & 7) * 16;
 #pragma unroll
             for (int c = 0; c < 4; c++)
               *reinterpret_cast<uint4*>(as + (wk * 4 + c) * kSbo) = expand8((w0 >> (8 * c)) & 0xffu, one);
           }
-#pragma unroll
-          for (int j = 0; j < kLook - 1; j++) wq[j] = wq[j + 1];
-          wq[kLook - 1] = wnew;
-#pragma unroll
-          for (int j = 0; j < kLook; j++) tq[j] = tq[j + 1];
-          int h = 0;
-          tq[kLook] = tq[kLook] >= 0 ? it.next(h) : -1;
-          if (tq[kLook] >= 0) seen |= h;
         }
         ptx::fence_proxy_async_smem();
         __syncwarp();
         if (lane == 0) ptx::mbar_arrive(&sm.full[s]);
+#pragma unroll
+        for (int j = 0; j < kWordAhead - 1; j++) wq[j] = wq[j + 1];
+        wq[kWordAhead - 1] = wnew;
       }
     }
   } else if (warp == kTmaWarp && lane == 0) {
     // ---------------- TMA issuer ----------------
-    StepIter it;
-    it.init(occ0, occ1, a.occ_words, dense_steps, dense_halves, MODE == kSddmm);
-    int h = 0;
-    int t = it.next(h);
-    for (int i = 0; t >= 0; i++) {
+    // Shared-memory addresses are formed once; a stage adds its offset.
+    const uint32_t a0 = ptx::smem_addr(sm.a[0]), b0 = ptx::smem_addr(sm.b[0]), f0 = ptx::smem_addr(&sm.full[0]);
+    for (int i = 0; i < nstages; i++) {
       const int s = i % kStages;
       if (i >= kStages && !ptx::mbar_wait(&sm.empty[s], ((i / kStages) - 1) & 1)) {
         atomicCAS(&g_tc_error, 0, 3);
@@ -313,41 +287,50 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
         break;
       }
       if (*(volatile int*)&sm.abort) break;
+      const uint32_t fb = f0 + s * 8, as = a0 + s * kStageBytes, bs = b0 + s * kStageBytes;
       if (MODE == kSddmm) {
-        // G rows row0.. and X rows col0.. (256 each), N columns t*64..
+        // G rows row0.. and X rows col0.. (256 each), N columns i*64..
         ptx::mbar_arrive_expect_tx(&sm.full[s], 2 * kStageBytes);
-        ptx::tma_load_2d(sm.a[s], &mapA, t * kSdK, (int)row0, &sm.full[s]);
-        ptx::tma_load_2d(sm.b[s], &mapB, t * kSdK, (int)col0, &sm.full[s]);
-        t = it.next(h);
+        ptx::tma_load_2d_u32(as, &mapA, i * kSdK, (int)row0, fb);
+        ptx::tma_load_2d_u32(bs, &mapB, i * kSdK, (int)col0, fb);
       } else {
-        // B (fwd) / G (trans) rows t*32.. of each of the stage's tiles,
-        // columns col0 + 64*j
-        const int t1 = it.next(h);
-        ptx::mbar_arrive_expect_tx(&sm.full[s], (t1 >= 0 ? 2 : 1) * kBTile);
+        // B (fwd) / G (trans) rows t*32.. of the stage's tiles, columns col0 + 64*j
+        const int k0 = kTilesPerStage * i;
+        const bool two = k0 + 1 < n;
+        const int t0 = sm.list[k0] & 0x0fffffff;
+        ptx::mbar_arrive_expect_tx(&sm.full[s], (two ? 2 : 1) * kBTile);
 #pragma unroll
         for (int j = 0; j < kTcN / kBoxCols; j++)
-          ptx::tma_load_2d(sm.b[s] + j * kBox, &mapB, (int)col0 + j * kBoxCols, t * kTcK, &sm.full[s]);
-        if (t1 >= 0) {
+          ptx::tma_load_2d_u32(bs + j * kBox, &mapB, (int)col0 + j * kBoxCols, t0 * kTcK, fb);
+        if (two) {
+          const int t1 = sm.list[k0 + 1] & 0x0fffffff;
 #pragma unroll
           for (int j = 0; j < kTcN / kBoxCols; j++)
-            ptx::tma_load_2d(sm.b[s] + kBTile + j * kBox, &mapB, (int)col0 + j * kBoxCols, t1 * kTcK, &sm.full[s]);
+            ptx::tma_load_2d_u32(bs + kBTile + j * kBox, &mapB, (int)col0 + j * kBoxCols, t1 * kTcK, fb);
         }
-        t = t1 >= 0 ? it.next(h) : -1;
       }
     }
   } else if (warp == kMmaWarp && lane == 0) {
     // ---------------- MMA issuer ----------------
+    // Descriptors of stage 0 are built once; every MMA adds a compile-time
+    // offset (plus the stage's) to the 14-bit start-address field (>> 4).
     const uint32_t ab = std::is_same<BT, __nv_bfloat16>::value ? 1u : 0u;
     const uint32_t idesc = idesc_f16(ab, MODE == kTrans ? 1u : 0u, MODE == kSddmm ? 0u : 1u);
-    StepIter it;
-    it.init(occ0, occ1, a.occ_words, dense_steps, dense_halves, MODE == kSddmm);
-    int i = 0, started = 0;
-    int hv[kTilesPerStage];
-    int t = it.next(hv[0]);
-    for (; t >= 0; i++) {
+    const uint32_t a0 = ptx::smem_addr(sm.a[0]), b0 = ptx::smem_addr(sm.b[0]);
+    const uint64_t adesc = MODE == kSddmm ? ptx::smem_desc_noswizzle_u32(a0, 16, kSdSbo) | ((uint64_t)kLayoutSw128 << 61)
+                                          : ptx::smem_desc_noswizzle_u32(a0, kLbo, kSbo);
+    const uint64_t bdesc = MODE == kSddmm ? ptx::smem_desc_noswizzle_u32(b0, 16, kSdSbo) | ((uint64_t)kLayoutSw128 << 61)
+                                          : ptx::smem_desc_noswizzle_u32(b0, kBox, 1024) | ((uint64_t)kLayoutSw128 << 61);
+    uint32_t started = 0;
+    int i = 0;
+    for (; i < nstages; i++) {
       const int s = i % kStages;
-      int nt = 1;
-      if (MODE != kSddmm) nt = it.next(hv[1]) >= 0 ? 2 : 1;
+      int hv0 = dense_halves, hv1 = 0;
+      if (MODE != kSddmm) {
+        const int k0 = kTilesPerStage * i;
+        hv0 = (sm.list[k0] >> 28) & 3;
+        hv1 = k0 + 1 < n ? (sm.list[k0 + 1] >> 28) & 3 : 0;
+      }
       if (!ptx::mbar_wait(&sm.full[s], (i / kStages) & 1)) {
         atomicCAS(&g_tc_error, 0, 3);
         sm.abort = 1;
@@ -355,51 +338,47 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
       }
       if (*(volatile int*)&sm.abort) break;
       ptx::tc_fence_after_sync();
+      const uint64_t soff = (uint64_t)((s * kStageBytes) >> 4);
+      const uint64_t as = adesc + soff, bs = bdesc + soff;
       if (MODE == kSddmm) {
 #pragma unroll
         for (int h = 0; h < kHalves; h++) {
-          if (!((hv[0] >> h) & 1)) continue;
+          if (!((hv0 >> h) & 1)) continue;
 #pragma unroll
-          for (int j = 0; j < kSdK / 16; j++) {
-            // both K-major, 128-byte swizzle; K step j starts 32 B into the rows
-            const uint64_t ad = ptx::smem_desc_swizzle(sm.a[s] + h * (kTcM * 128) + j * 32, 16, kSdSbo, kLayoutSw128);
-            const uint64_t bd = ptx::smem_desc_swizzle(sm.b[s] + j * 32, 16, kSdSbo, kLayoutSw128);
-            ptx::tc_mma_f16(tmem + (uint32_t)(h * kTcN), ad, bd, idesc, ((started >> h) & 1) || (j > 0));
-          }
-          started |= 1 << h;
+          for (int j = 0; j < kSdK / 16; j++)  // K step j starts 32 B into the 128-byte rows
+            ptx::tc_mma_f16(tmem + (uint32_t)(h * kTcN), as + (uint64_t)((h * kTcM * 128 + j * 32) >> 4),
+                            bs + (uint64_t)((j * 32) >> 4), idesc, ((started >> h) & 1u) || j > 0);
+          started |= 1u << h;
         }
       } else {
 #pragma unroll
         for (int u = 0; u < kTilesPerStage; u++) {
-          if (u >= nt) break;
+          const int hv = u == 0 ? hv0 : hv1;
 #pragma unroll
           for (int h = 0; h < kHalves; h++) {
-            if (!((hv[u] >> h) & 1)) continue;
+            if (!((hv >> h) & 1)) continue;
 #pragma unroll
-            for (int j = 0; j < 2; j++) {
-              // A: core matrices; B: 128-byte swizzle, K half j = two 8-row groups on
-              const uint64_t ad =
-                  ptx::smem_desc_noswizzle(sm.a[s] + u * kATile + h * kAHalf + j * 2 * kLbo, kLbo, kSbo);
-              const uint64_t bd = ptx::smem_desc_swizzle(sm.b[s] + u * kBTile + j * 2 * 1024, kBox, 1024, kLayoutSw128);
-              ptx::tc_mma_f16(tmem + (uint32_t)(h * kTcN), ad, bd, idesc, ((started >> h) & 1) || (j > 0));
-            }
-            started |= 1 << h;
+            for (int j = 0; j < 2; j++)  // K half j: A two core-matrix columns on, B two 8-row groups on
+              ptx::tc_mma_f16(tmem + (uint32_t)(h * kTcN),
+                              as + (uint64_t)((u * kATile + h * kAHalf + j * 2 * kLbo) >> 4),
+                              bs + (uint64_t)((u * kBTile + j * 2 * 1024) >> 4), idesc, ((started >> h) & 1u) || j > 0);
+            started |= 1u << h;
           }
         }
       }
       ptx::tc_commit(&sm.empty[s]);
-      t = (MODE == kSddmm || nt == 2) ? it.next(hv[0]) : -1;
     }
     if (i > 0) ptx::tc_commit(&sm.done);
     else ptx::mbar_arrive(&sm.done);
   }
 
   // ---------------- epilogue (producer warps) ----------------
-  // Warp w reads TMEM lanes 32*(w%4).. of accumulator w/4 (a warp may only
-  // touch its own quarter of the lanes); a thread owns one output row.
+  // Warp w reads TMEM lanes 32*(w%4).. (a warp may only touch its own
+  // quarter of the lanes) of accumulator (w/4)%2, columns 128*(w/8)..; a
+  // thread stores 128 columns of one output row.
   if (warp < kProducerWarps) {
-    const int h = warp >> 2, q = warp & 3;
-    const bool have = (seen >> h) & 1;
+    const int h = (warp >> 2) & 1, q = warp & 3, cg = warp >> 3;
+    const bool have = (sm.seen >> h) & 1;
     bool ok = ptx::mbar_wait(&sm.done, 0);
     if (!ok) {
       atomicCAS(&g_tc_error, 0, 3);
@@ -407,11 +386,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
     }
     ptx::tc_fence_after_sync();
     const int64_t row = row0 + h * kTcM + q * 32 + lane;
-    float* crow = a.C + row * a.ldc + col0;
+    float* crow = a.C + row * a.ldc + col0 + cg * (kTcN / 2);
     const bool live = row < out_rows && ok && !*(volatile int*)&sm.abort;
     const uint32_t* arow = a.A + row * a.Kw;
-    const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * kTcN);
-    for (int c8 = 0; c8 < kTcN / 8; c8 += 4) {
+    const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * kTcN + cg * (kTcN / 2));
+    for (int c8 = 0; c8 < kTcN / 16; c8 += 4) {
       uint32_t r[4][8];
       if (have && ok) {
 #pragma unroll
@@ -427,9 +406,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
 #pragma unroll
       for (int u = 0; u < 4; u++) {
         const int col = (c8 + u) * 8;
-        if (col0 + col >= out_cols) continue;
+        const int64_t gcol = col0 + cg * (kTcN / 2) + col;
+        if (gcol >= out_cols) continue;
         if (MODE == kSddmm) {  // keep the set bits of A's row only
-          const uint32_t bits = (__ldg(arow + (col0 + col) / 32) >> ((col0 + col) & 31)) & 0xffu;
+          const uint32_t bits = (__ldg(arow + gcol / 32) >> (gcol & 31)) & 0xffu;
 #pragma unroll
           for (int v = 0; v < 8; v++)
             if (!((bits >> v) & 1u)) r[u][v] = 0u;
@@ -498,6 +478,7 @@ __global__ void __launch_bounds__(256) k_tile_occupancy(const uint32_t* __restri
 }  // namespace
 
 int tc_occupancy_words(int64_t K) { return (int)ceil_div(ceil_div(K, 32), 32); }
+int64_t tc_max_reduction() { return (int64_t)kListMax * kTcK; }
 int tc_occupancy_t_words(int64_t M) { return (int)ceil_div(ceil_div(M, 32), 32); }
 
 int launch_tile_occupancy(const uint32_t* A, int64_t M, int64_t K, uint32_t* occ,
@@ -580,6 +561,8 @@ int launch_tc(const TcArgs& a, cudaStream_t s) {
   const dim3 grid((unsigned)ceil_div(rows, kCtaM), (unsigned)ceil_div(cols, kTcN));
   if (ceil_div(cols, kTcN) > 65535 || ceil_div(rows, kCtaM) > 0x7fffffff) return BSP_ERR_CAPACITY;
   if (a.N > INT32_MAX || a.M > INT32_MAX || a.K > INT32_MAX) return BSP_ERR_CAPACITY;
+  // the tile list of a CTA holds every reduction tile (fwd: K, trans: M)
+  if (MODE != kSddmm && ceil_div(MODE == kFwd ? a.K : a.M, kTcK) > kListMax) return BSP_ERR_CAPACITY;
   CUtensorMap ma, mb;
   memset(&ma, 0, sizeof(ma));
   if (MODE == kSddmm) {
