@@ -69,7 +69,6 @@ constexpr int kListMax = 4096;
 constexpr uint32_t kTmemCols = 512;       // two 128x256 FP32 accumulators
 using tc::kLbo;
 using tc::kSbo;
-using tc::expand8;
 using tc::kLayoutSw128;
 constexpr int kFwd = 0, kTrans = 1, kSddmm = 2;
 // B (fwd) / G (trans) tile: four TMA boxes of 64 columns x 32 reduction rows,
@@ -137,7 +136,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
   const int64_t col0 = (int64_t)blockIdx.y * kTcN;   // output columns: N (fwd, trans) or K (sddmm)
   const int64_t out_rows = MODE == kTrans ? a.K : a.M;
   const int64_t out_cols = MODE == kSddmm ? a.K : a.N;
-  const uint32_t one = std::is_same<BT, __nv_bfloat16>::value ? 0x3f80u : 0x3c00u;
   const int dense_halves = row0 + kTcM < out_rows ? 3 : 1;
 
   if (tid == 0) {
@@ -252,19 +250,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
         if (!__shfl_sync(kFull, go, 0)) break;
         if (kTilesPerStage * i + u < n) {
           uint8_t* at = sm.a[s] + u * kATile;
+          uint4 e[4];
+          tc::expand32_two(w0, e);
           if (MODE == kFwd) {
             // row r of the tile: half r/128 at 8 KB, then core matrices
             uint8_t* as = at + (r >> 3) * kSbo + (r & 7) * 16;
 #pragma unroll
-            for (int c = 0; c < 4; c++)
-              *reinterpret_cast<uint4*>(as + c * kLbo) = expand8((w0 >> (8 * c)) & 0xffu, one);
+            for (int c = 0; c < 4; c++) *reinterpret_cast<uint4*>(as + c * kLbo) = e[c];
           } else {
             // A row j of the tile, word wk of the block: output rows wk*32 + 8c ..
             const int j = r & 31, wk = r >> 5;
             uint8_t* as = at + (j >> 3) * kLbo + (j & 7) * 16;
 #pragma unroll
-            for (int c = 0; c < 4; c++)
-              *reinterpret_cast<uint4*>(as + (wk * 4 + c) * kSbo) = expand8((w0 >> (8 * c)) & 0xffu, one);
+            for (int c = 0; c < 4; c++) *reinterpret_cast<uint4*>(as + (wk * 4 + c) * kSbo) = e[c];
           }
         }
         ptx::fence_proxy_async_smem();
@@ -413,6 +411,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
 #pragma unroll
           for (int v = 0; v < 8; v++)
             if (!((bits >> v) & 1u)) r[u][v] = 0u;
+        } else {  // the bit operand held 2.0 per set bit
+#pragma unroll
+          for (int v = 0; v < 8; v++) r[u][v] = __float_as_uint(__uint_as_float(r[u][v]) * tc::kTwoScale);
         }
         *reinterpret_cast<float4*>(crow + col) = make_float4(
             __uint_as_float(r[u][0]), __uint_as_float(r[u][1]), __uint_as_float(r[u][2]), __uint_as_float(r[u][3]));

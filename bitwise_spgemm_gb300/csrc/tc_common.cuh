@@ -37,6 +37,33 @@ __host__ __device__ constexpr uint32_t idesc_f16(uint32_t ab_type, uint32_t a_mn
          ((m >> 4) << 24);
 }
 
+// 32 bits of a word → 32 16-bit values, 2.0 for a set bit and 0 otherwise,
+// as four 16-byte chunks of 8 consecutive values (value i = bit i).  2.0 is
+// 0x4000 in BF16 and FP16 alike: one set bit, so after the word is
+// unshuffled (even bits to the low half, odd bits to the high half — the
+// perfect-unshuffle of Hacker's Delight, section 7-2) the pair of values
+// 2j, 2j+1 is one shift and one mask.  Products made with 2.0 are scaled by
+// 0.5 when stored, which is exact in binary floating point (unless a sum
+// exceeds half the FP32 range).
+constexpr float kTwoScale = 0.5f;
+__device__ __forceinline__ void expand32_two(uint32_t w, uint4 (&o)[4]) {
+  uint32_t x = w, t;
+  t = (x ^ (x >> 1)) & 0x22222222u;
+  x ^= t ^ (t << 1);
+  t = (x ^ (x >> 2)) & 0x0c0c0c0cu;
+  x ^= t ^ (t << 2);
+  t = (x ^ (x >> 4)) & 0x00f000f0u;
+  x ^= t ^ (t << 4);
+  t = (x ^ (x >> 8)) & 0x0000ff00u;
+  x ^= t ^ (t << 8);
+  // x: bit j = bit 2j of w, bit 16+j = bit 2j+1 of w (j < 16)
+  uint32_t v[16];
+#pragma unroll
+  for (int j = 0; j < 16; j++) v[j] = (j <= 14 ? (x << (14 - j)) : (x >> (j - 14))) & 0x40004000u;
+#pragma unroll
+  for (int c = 0; c < 4; c++) o[c] = make_uint4(v[4 * c], v[4 * c + 1], v[4 * c + 2], v[4 * c + 3]);
+}
+
 // 8 bits of a word → 8 16-bit values 0 / one, packed little-endian.
 __device__ __forceinline__ uint4 expand8(uint32_t byte, uint32_t one) {
   uint32_t w[4];
