@@ -74,6 +74,15 @@ SIGNATURES = {
     "bsp_batched_spmm": [_P, _P],
     "bsp_spmm_t": [_P, _I64, _I64, _P, _I, _I64, _I64, _P, _I64, _P, _P, _SZ, _P],
     "bsp_sddmm": [_P, _I64, _I64, _P, _I64, _P, _I64, _I, _I64, _P, _I64, _P, _P],
+    "bsp_symbolic_rows": [_P, _I64, _I64, _P, _I64, _P, _P],
+    "bsp_bitplane_spmm": [_P, _I, _I, _I64, _I64, _P, _I, _I64, _I64, _P, _I64, _P],
+    "bsp_spmm_i8_workspace": [_I64, _I64, C.POINTER(_SZ)],
+    "bsp_spmm_i8": [_P, _I64, _I64, _I64, _P, _I, _I64, _I64, _P, _I64, _P, _SZ, _P],
+    "bsp_tiles8_workspace": [_I64, _I64, C.POINTER(_SZ)],
+    "bsp_rows_to_tiles8": [_P, _I64, _I64, _P, _P, _P, _P, _P, _P, _SZ, _P],
+    "bsp_tiles8_to_rows": [_P, _P, _P, _I64, _I64, _I64, _P, _P],
+    "bsp_csr_to_tiled_workspace": [_I64, _I64, _I64, _I, _I, C.POINTER(_SZ)],
+    "bsp_csr_to_tiled": [_P, _P, _P, _I, _I64, _I64, _I64, _I, _I, _P, _P, _P, _P, _P, _SZ, _P],
     "bsp_spmm_noalloc": [_P, _I64, _I64, _P, _I, _I64, _I64, _P, _I64, _P, _P],
 }
 _RESTYPES = {"bsp_status_string": C.c_char_p}

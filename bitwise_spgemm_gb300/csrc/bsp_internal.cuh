@@ -71,6 +71,22 @@ int launch_group_to_dense(const float* gv, const int32_t* gid, const uint32_t* w
 // Exclusive prefix sum of n int32 values into out[0..n] (out[n] = total).
 // ws must hold scan_workspace_bytes(n) bytes.
 size_t scan_workspace_bytes(int64_t n);
+// formats.cu
+size_t tiles8_workspace_bytes(int64_t M, int64_t K);
+int launch_rows_to_tiles8(const uint32_t* words, int64_t M, int64_t K, uint64_t* bmp, int32_t* trow, int32_t* tcol,
+                          int32_t* offset, int64_t* n_tiles, void* ws, cudaStream_t s);
+int launch_tiles8_to_rows(const uint64_t* bmp, const int32_t* trow, const int32_t* tcol, int64_t n, int64_t M,
+                          int64_t K, uint32_t* words, cudaStream_t s);
+size_t csr_tiled_workspace_bytes(int64_t M, int64_t K, int64_t nnz, int tile_rows, int tile_cols);
+int launch_csr_to_tiled(const int32_t* row_ptr, const int32_t* col, const void* val, int vbytes, int64_t M,
+                        int64_t K, int64_t nnz, int tr, int tc, int32_t* acc, int32_t* toff, int32_t* tcol,
+                        void* tval, void* ws, cudaStream_t s);
+// output.cu
+int launch_symbolic_rows(const uint32_t* A, int64_t M, int64_t K, const uint32_t* Bw, int64_t N, uint32_t* Cw,
+                         cudaStream_t s);
+int launch_bitplane_spmm(const uint32_t* planes, int nplanes, int signed_top, int64_t M, int64_t K,
+                         const void* B, int bdt, int64_t ldb, int64_t N, float* C, int64_t ldc, bool vec,
+                         cudaStream_t s);
 int launch_scan_i32(const int32_t* in, int64_t n, int32_t* out, void* ws, cudaStream_t s);
 
 }  // namespace bsp

@@ -329,6 +329,128 @@ int bsp_spmm(const uint32_t* A_words, int64_t M, int64_t K, const void* B, int b
   return launch_spmm_rows(a, proto, vec, s);
 }
 
+int bsp_symbolic_rows(const uint32_t* A_words, int64_t M, int64_t K, const uint32_t* B_words, int64_t N,
+                      uint32_t* C_words, bsp_stream_t stream) {
+  BSP_TRY(check_dims(M, K));
+  if (N < 0 || N > kMaxCols) return BSP_ERR_INVALID_ARG;
+  if (M == 0 || N == 0) return BSP_OK;
+  if (!C_words || (K > 0 && (!A_words || !B_words))) return BSP_ERR_INVALID_ARG;
+  if (!is_aligned(A_words, 4) || !is_aligned(B_words, 4) || !is_aligned(C_words, 4)) return BSP_ERR_ALIGNMENT;
+  const cudaStream_t s = (cudaStream_t)stream;
+  if (K == 0) {
+    BSP_CUDA(cudaMemsetAsync(C_words, 0, sizeof(uint32_t) * (size_t)M * (size_t)ceil_div(N, 32), s));
+    return BSP_OK;
+  }
+  return launch_symbolic_rows(A_words, M, K, B_words, N, C_words, s);
+}
+
+static bool layout16(const void* p, int64_t ld, int esz, int64_t N, int vcols);
+
+int bsp_bitplane_spmm(const uint32_t* planes, int n_planes, int is_signed, int64_t M, int64_t K, const void* B,
+                      int b_dtype, int64_t ldb, int64_t N, float* C, int64_t ldc, bsp_stream_t stream) {
+  BSP_TRY(check_dims(M, K));
+  if (n_planes < 1 || n_planes > 8) return BSP_ERR_INVALID_ARG;
+  if (N < 0 || N > kMaxCols || ldb < N || ldc < N) return BSP_ERR_INVALID_ARG;
+  if (b_dtype != BSP_F32 && b_dtype != BSP_BF16 && b_dtype != BSP_F16) return BSP_ERR_UNSUPPORTED;
+  if (M == 0 || N == 0) return BSP_OK;
+  if (!C || (K > 0 && (!planes || !B))) return BSP_ERR_INVALID_ARG;
+  const int esz = dtype_size(b_dtype);
+  if (!is_aligned(B, esz) || !is_aligned(C, 4) || !is_aligned(planes, 4)) return BSP_ERR_ALIGNMENT;
+  const cudaStream_t s = (cudaStream_t)stream;
+  if (K == 0) {
+    BSP_CUDA(cudaMemset2DAsync(C, sizeof(float) * ldc, 0, sizeof(float) * N, M, s));
+    return BSP_OK;
+  }
+  const int vcols = b_dtype == BSP_F32 ? 4 : 8;
+  const bool vec = layout16(B, ldb, esz, N, vcols) && layout16(C, ldc, 4, N, 4);
+  return launch_bitplane_spmm(planes, n_planes, is_signed != 0, M, K, B, b_dtype, ldb, N, C, ldc, vec, s);
+}
+
+int bsp_spmm_i8_workspace(int64_t M, int64_t K, size_t* bytes) {
+  if (!bytes || M < 0 || K < 0) return BSP_ERR_INVALID_ARG;
+  *bytes = sizeof(uint32_t) * 8 * (size_t)M * (size_t)ceil_div(K, 32) + 256;
+  return BSP_OK;
+}
+
+int bsp_spmm_i8(const int8_t* A, int64_t M, int64_t K, int64_t lda, const void* B, int b_dtype, int64_t ldb,
+                int64_t N, float* C, int64_t ldc, void* workspace, size_t workspace_bytes, bsp_stream_t stream) {
+  BSP_TRY(check_dims(M, K));
+  if (lda < K) return BSP_ERR_INVALID_ARG;
+  if (M == 0 || N == 0) return BSP_OK;
+  if (K > 0 && !A) return BSP_ERR_INVALID_ARG;
+  size_t need = 0;
+  BSP_TRY(bsp_spmm_i8_workspace(M, K, &need));
+  uint32_t* planes = nullptr;
+  if (K > 0) {
+    if (!workspace || workspace_bytes < need) return BSP_ERR_WORKSPACE;
+    planes = reinterpret_cast<uint32_t*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~(uintptr_t)255);
+    BSP_TRY(bsp_bitplanes(reinterpret_cast<const uint8_t*>(A), M, K, lda, 8, planes, BSP_LSB_FIRST, stream));
+  }
+  return bsp_bitplane_spmm(planes, 8, 1, M, K, B, b_dtype, ldb, N, C, ldc, stream);
+}
+
+int bsp_tiles8_workspace(int64_t M, int64_t K, size_t* bytes) {
+  if (!bytes || M < 0 || K < 0) return BSP_ERR_INVALID_ARG;
+  *bytes = tiles8_workspace_bytes(M, K) + 256;
+  return BSP_OK;
+}
+
+int bsp_rows_to_tiles8(const uint32_t* words, int64_t M, int64_t K, uint64_t* bmp, int32_t* tile_row,
+                       int32_t* tile_col, int32_t* offset, int64_t* n_tiles, void* workspace, size_t workspace_bytes,
+                       bsp_stream_t stream) {
+  BSP_TRY(check_dims(M, K));
+  if (M * K >= ((int64_t)1 << 31)) return BSP_ERR_CAPACITY;
+  if (!n_tiles || !offset) return BSP_ERR_INVALID_ARG;
+  if (!is_aligned(n_tiles, 8) || !is_aligned(offset, 4)) return BSP_ERR_ALIGNMENT;
+  const cudaStream_t s = (cudaStream_t)stream;
+  if (M == 0 || K == 0) {
+    BSP_CUDA(cudaMemsetAsync(n_tiles, 0, sizeof(int64_t), s));
+    BSP_CUDA(cudaMemsetAsync(offset, 0, sizeof(int32_t), s));
+    return BSP_OK;
+  }
+  if (!words || !bmp || !tile_row || !tile_col) return BSP_ERR_INVALID_ARG;
+  if (!is_aligned(words, 4) || !is_aligned(bmp, 8) || !is_aligned(tile_row, 4) || !is_aligned(tile_col, 4))
+    return BSP_ERR_ALIGNMENT;
+  size_t need = 0;
+  BSP_TRY(bsp_tiles8_workspace(M, K, &need));
+  if (!workspace || workspace_bytes < need) return BSP_ERR_WORKSPACE;
+  return launch_rows_to_tiles8(words, M, K, bmp, tile_row, tile_col, offset, n_tiles, workspace, s);
+}
+
+int bsp_tiles8_to_rows(const uint64_t* bmp, const int32_t* tile_row, const int32_t* tile_col, int64_t n_tiles,
+                       int64_t M, int64_t K, uint32_t* words, bsp_stream_t stream) {
+  BSP_TRY(check_dims(M, K));
+  if (n_tiles < 0 || n_tiles > ((int64_t)1 << 40)) return BSP_ERR_INVALID_ARG;
+  if (M == 0 || K == 0) return BSP_OK;
+  if (!words || (n_tiles > 0 && (!bmp || !tile_row || !tile_col))) return BSP_ERR_INVALID_ARG;
+  if (!is_aligned(words, 4) || !is_aligned(bmp, 8) || !is_aligned(tile_row, 4) || !is_aligned(tile_col, 4))
+    return BSP_ERR_ALIGNMENT;
+  return launch_tiles8_to_rows(bmp, tile_row, tile_col, n_tiles, M, K, words, (cudaStream_t)stream);
+}
+
+int bsp_csr_to_tiled_workspace(int64_t M, int64_t K, int64_t nnz, int tile_rows, int tile_cols, size_t* bytes) {
+  if (!bytes || M < 0 || K < 0 || nnz < 0 || tile_rows < 1 || tile_cols < 1) return BSP_ERR_INVALID_ARG;
+  *bytes = csr_tiled_workspace_bytes(M, K, nnz, tile_rows, tile_cols) + 256;
+  return BSP_OK;
+}
+
+int bsp_csr_to_tiled(const int32_t* row_ptr, const int32_t* col_idx, const void* values, int value_bytes, int64_t M,
+                     int64_t K, int64_t nnz, int tile_rows, int tile_cols, int32_t* tile_nnz_acc,
+                     int32_t* tiled_offset, int32_t* tiled_col, void* tiled_values, void* workspace,
+                     size_t workspace_bytes, bsp_stream_t stream) {
+  BSP_TRY(check_dims(M, K));
+  if (nnz < 0 || tile_rows < 1 || tile_cols < 1 || value_bytes < 0 || value_bytes > 8) return BSP_ERR_INVALID_ARG;
+  if (nnz >= ((int64_t)1 << 31)) return BSP_ERR_CAPACITY;
+  if (M == 0 || K == 0) return BSP_OK;
+  if (!row_ptr || !tile_nnz_acc || !tiled_offset || (nnz > 0 && (!col_idx || !tiled_col))) return BSP_ERR_INVALID_ARG;
+  if ((values != nullptr) != (tiled_values != nullptr) || (values && value_bytes == 0)) return BSP_ERR_INVALID_ARG;
+  size_t need = 0;
+  BSP_TRY(bsp_csr_to_tiled_workspace(M, K, nnz, tile_rows, tile_cols, &need));
+  if (!workspace || workspace_bytes < need) return BSP_ERR_WORKSPACE;
+  return launch_csr_to_tiled(row_ptr, col_idx, values, value_bytes, M, K, nnz, tile_rows, tile_cols, tile_nnz_acc,
+                             tiled_offset, tiled_col, tiled_values, workspace, (cudaStream_t)stream);
+}
+
 int bsp_spmm_t_workspace(int64_t M, int64_t K, size_t* bytes) {
   if (!bytes || M < 0 || K < 0) return BSP_ERR_INVALID_ARG;
   *bytes = sizeof(uint32_t) * (size_t)K * (size_t)ceil_div(M, 32) + 256;

@@ -1,0 +1,183 @@
+// output.cu — the steps around the SpMM when the operands are themselves
+// bitmaps or multi-bit values:
+//
+//  * symbolic output masks: for A (M×K) and B (K×N) both given as packed
+//    bit rows, row i of C's mask is the OR of B's row masks at A's set bits
+//    (the symbolic half of pre_spgemm, reference source/src/transform.cuh:
+//    1028-1057, which walked a CSR copy of A one thread per row and kept the
+//    mask in shared memory).  The first-fit grouping of the output rows that
+//    follows it there is bsp_group_rows on the result.
+//  * bit-plane products: C = Σ_b w_b · (P_b · B) for the 0/1 planes P_b of
+//    an 8-bit matrix, w_b = 2^b and, for two's complement values, −2^7 for
+//    the top plane — the recombination of spgemm_compute_1dthread_tcore_v3
+//    (transform.cuh:2199-2246) with the weights of initialize_multiplicand
+//    (main.cu:895-910).  There every plane went through a wmma tile of half
+//    values and shared-memory atomics; here one warp walks the planes of a
+//    row, sums each plane in FP32 (TwoSum compensated) and adds it, scaled by
+//    its power-of-two weight (exact), to the row's total.
+#include "ptx.cuh"
+#include "spmm_dev.cuh"
+
+namespace bsp {
+namespace {
+
+constexpr int kSymWords = 4;  // output words per lane (128 per warp)
+constexpr int kSymDepth = 8;  // B row masks in flight per warp
+
+// One warp per (row of C, 128-word chunk of its mask).  The walker yields
+// A's set bits in ascending order; columns at or past K (stray bits in the
+// padding of A's last word) are ignored.
+__global__ void __launch_bounds__(256) k_symbolic_rows(const uint32_t* __restrict__ A, int64_t M, int64_t K,
+                                                       int64_t Kw, const uint32_t* __restrict__ Bw, int64_t Nw,
+                                                       uint32_t* __restrict__ Cw) {
+  const int lane = threadIdx.x & 31;
+  const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (row >= M) return;
+  const int64_t w0 = (int64_t)blockIdx.y * (32 * kSymWords);
+  uint32_t acc[kSymWords] = {};
+  BitWalker wk;
+  wk.init(A + row * Kw, 0, (int)Kw, lane);
+  while (true) {
+    uint32_t idx[kSymDepth];
+#pragma unroll
+    for (int s = 0; s < kSymDepth; s++) idx[s] = wk.next();
+    if (idx[0] == kEnd) break;
+    uint32_t v[kSymDepth][kSymWords];
+#pragma unroll
+    for (int s = 0; s < kSymDepth; s++)
+#pragma unroll
+      for (int q = 0; q < kSymWords; q++) {
+        const int64_t w = w0 + q * 32 + lane;
+        v[s][q] = (idx[s] != kEnd && (int64_t)idx[s] < K && w < Nw) ? __ldg(Bw + (int64_t)idx[s] * Nw + w) : 0u;
+      }
+#pragma unroll
+    for (int s = 0; s < kSymDepth; s++)
+#pragma unroll
+      for (int q = 0; q < kSymWords; q++) acc[q] |= v[s][q];
+    if (idx[kSymDepth - 1] == kEnd) break;
+  }
+#pragma unroll
+  for (int q = 0; q < kSymWords; q++) {
+    const int64_t w = w0 + q * 32 + lane;
+    if (w < Nw) Cw[row * Nw + w] = acc[q];
+  }
+}
+
+struct PlaneArgs {
+  const uint32_t* planes;  // [nplanes][M][Kw]
+  int64_t M, K, Kw;
+  int nplanes, signed_top;
+  const void* B;
+  int64_t ldb, N;
+  float* C;
+  int64_t ldc;
+};
+
+__device__ __forceinline__ float plane_weight(int b, int nplanes, int signed_top) {
+  const float w = (float)(1u << b);
+  return (signed_top && b == nplanes - 1) ? -w : w;
+}
+
+// One warp per (row, column chunk of 32*VPL*COLS), 16-byte vectors of B.
+template <typename BT, int VPL, int D>
+__global__ void __launch_bounds__(256) k_bitplane_rows(PlaneArgs a) {
+  using V = Vec<BT>;
+  constexpr int COLS = V::COLS;
+  constexpr int CW = 32 * VPL * COLS;
+  const int lane = threadIdx.x & 31;
+  const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (row >= a.M) return;
+  const int n0 = (int)blockIdx.y * CW;
+  const BT* __restrict__ B = static_cast<const BT*>(a.B);
+  int col[VPL];
+  bool cvalid[VPL];
+#pragma unroll
+  for (int v = 0; v < VPL; v++) {
+    col[v] = n0 + (v * 32 + lane) * COLS;
+    cvalid[v] = col[v] < a.N;
+  }
+  Acc<VPL, COLS, false> tot;
+  tot.zero();
+  for (int b = 0; b < a.nplanes; b++) {
+    BitWalker wk;
+    wk.init(a.planes + ((int64_t)b * a.M + row) * a.Kw, 0, (int)a.Kw, lane);
+    Acc<VPL, COLS, true> acc;
+    acc.zero();
+    accumulate_walk<BT, VPL, D, true>(wk, B, a.ldb, col, cvalid, acc);
+    const float w = plane_weight(b, a.nplanes, a.signed_top);
+#pragma unroll
+    for (int v = 0; v < VPL; v++)
+#pragma unroll
+      for (int j = 0; j < COLS; j++) tot.s[v][j] += w * acc.result(v, j);
+  }
+  store_vecs<VPL, COLS, false>(a.C + row * a.ldc, col, cvalid, tot, nullptr);
+}
+
+// Any layout: one warp per (row, 32 columns), a lane per column.
+template <typename BT>
+__global__ void __launch_bounds__(256) k_bitplane_rows_scalar(PlaneArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (row >= a.M) return;
+  const BT* __restrict__ B = static_cast<const BT*>(a.B);
+  for (int64_t c0 = (int64_t)blockIdx.y * 32; c0 < a.N; c0 += (int64_t)gridDim.y * 32) {
+    const int64_t c = c0 + lane;
+    float tot = 0.f;
+    for (int b = 0; b < a.nplanes; b++) {
+      BitWalker wk;
+      wk.init(a.planes + ((int64_t)b * a.M + row) * a.Kw, 0, (int)a.Kw, lane);
+      float s = 0.f, e = 0.f;
+      for (uint32_t k = wk.next(); k != kEnd; k = wk.next()) {
+        const float x = c < a.N ? to_f32(B[(int64_t)k * a.ldb + c]) : 0.f;
+        const float t = s + x, bp = t - s;
+        e += (s - (t - bp)) + (x - bp);
+        s = t;
+      }
+      tot += plane_weight(b, a.nplanes, a.signed_top) * (s + e);
+    }
+    if (c < a.N) a.C[row * a.ldc + c] = tot;
+  }
+}
+
+template <typename BT>
+int launch_planes_t(const PlaneArgs& a, bool vec, cudaStream_t s) {
+  const unsigned gx = (unsigned)ceil_div(a.M, 8);
+  if (!vec) {
+    const int64_t gy = ceil_div(a.N, 32) < 65535 ? ceil_div(a.N, 32) : 65535;
+    k_bitplane_rows_scalar<BT><<<dim3(gx, (unsigned)gy), 256, 0, s>>>(a);
+  } else {
+    constexpr int COLS = Vec<BT>::COLS;
+    constexpr int VPL = COLS == 4 ? 2 : 1;
+    const int64_t gy = ceil_div(a.N, 32 * VPL * COLS);
+    if (gy > 65535) return BSP_ERR_CAPACITY;
+    k_bitplane_rows<BT, VPL, 8><<<dim3(gx, (unsigned)gy), 256, 0, s>>>(a);
+  }
+  BSP_LAUNCHED();
+  return BSP_OK;
+}
+
+}  // namespace
+
+int launch_symbolic_rows(const uint32_t* A, int64_t M, int64_t K, const uint32_t* Bw, int64_t N, uint32_t* Cw,
+                         cudaStream_t s) {
+  const int64_t Kw = ceil_div(K, 32), Nw = ceil_div(N, 32);
+  const int64_t gy = ceil_div(Nw, 32 * kSymWords);
+  if (M == 0 || Nw == 0) return BSP_OK;
+  if (gy > 65535) return BSP_ERR_CAPACITY;
+  k_symbolic_rows<<<dim3((unsigned)ceil_div(M, 8), (unsigned)gy), 256, 0, s>>>(A, M, K, Kw, Bw, Nw, Cw);
+  BSP_LAUNCHED();
+  return BSP_OK;
+}
+
+int launch_bitplane_spmm(const uint32_t* planes, int nplanes, int signed_top, int64_t M, int64_t K,
+                         const void* B, int bdt, int64_t ldb, int64_t N, float* C, int64_t ldc, bool vec,
+                         cudaStream_t s) {
+  if (M == 0 || N == 0) return BSP_OK;
+  PlaneArgs a = {planes, M, K, ceil_div(K, 32), nplanes, signed_top, B, ldb, N, C, ldc};
+  if (bdt == BSP_F32) return launch_planes_t<float>(a, vec, s);
+  if (bdt == BSP_BF16) return launch_planes_t<__nv_bfloat16>(a, vec, s);
+  if (bdt == BSP_F16) return launch_planes_t<__half>(a, vec, s);
+  return BSP_ERR_UNSUPPORTED;
+}
+
+}  // namespace bsp

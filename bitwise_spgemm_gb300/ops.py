@@ -205,6 +205,109 @@ def sddmm(words, M, K, G, X, plan=None, out=None):
     return out
 
 
+def symbolic_rows(a_words, K, b_words, N, out=None):
+    """Bit pattern of A·B for two bit matrices: row i of the result [M,
+    ceil(N/32)] is the OR of B's row masks at A's set bits.  The symbolic
+    half of pre_spgemm (reference source/src/transform.cuh:1028-1057);
+    group_rows on the result is its output grouping."""
+    M = a_words.shape[0]
+    if b_words.shape[0] != K:
+        raise ValueError("b_words must have K rows")
+    if out is None:
+        out = torch.empty((M, words_per_row(N)), dtype=torch.int32, device=a_words.device)
+    call("bsp_symbolic_rows", _p(a_words), M, K, _p(b_words), N, _p(out), _stream())
+    return out
+
+
+def bitplane_spmm(planes, K, B, signed=True, out=None):
+    """C = sum_b w_b (P_b B) for packed bit planes [n_planes, M, ceil(K/32)]
+    (as ``bitplanes`` returns them), w_b = 2^b and -2^(n-1) for the top plane
+    when ``signed``.  Replaces the bit-serial int8 product of
+    spgemm_compute_1dthread_tcore_v3 (transform.cuh:2199-2246)."""
+    n_planes, M, _ = planes.shape
+    ldb = _rowmajor(B, "B")
+    if B.shape[0] != K:
+        raise ValueError("B must have K rows")
+    N = B.shape[1]
+    if out is None:
+        out = torch.empty((M, N), dtype=torch.float32, device=B.device)
+    call("bsp_bitplane_spmm", _p(planes), n_planes, int(signed), M, K, _p(B), _DT[B.dtype], ldb, N,
+         _p(out), out.stride(0), _stream())
+    return out
+
+
+def spmm_i8(A, B, out=None, workspace=None):
+    """C = A·B for a dense int8 A [M, K]: bit planes in a workspace, then the
+    signed bit-plane product (the reference's layout_trans + bit-serial path)."""
+    lda = _rowmajor(A, "A")
+    if A.dtype != torch.int8:
+        raise ValueError("A must be int8")
+    M, K = A.shape
+    ldb = _rowmajor(B, "B")
+    N = B.shape[1]
+    if out is None:
+        out = torch.empty((M, N), dtype=torch.float32, device=B.device)
+    need = C.c_size_t(0)
+    call("bsp_spmm_i8_workspace", M, K, C.byref(need))
+    if workspace is None or workspace.numel() * workspace.element_size() < need.value:
+        workspace = torch.empty(need.value, dtype=torch.uint8, device=B.device)
+    call("bsp_spmm_i8", _p(A), M, K, lda, _p(B), _DT[B.dtype], ldb, N, _p(out), out.stride(0),
+         _p(workspace), workspace.numel() * workspace.element_size(), _stream())
+    return out
+
+
+def _ws(fn, *args, device):
+    need = C.c_size_t(0)
+    call(fn, *args, C.byref(need))
+    return torch.empty(max(need.value, 1), dtype=torch.uint8, device=device)
+
+
+def rows_to_tiles8(words, K):
+    """Packed rows [M, ceil(K/32)] -> the tSparse 8x8 bitmap tiles
+    (reference coo2bmp_noTuple_d, source/src/main.cu:692-779): returns
+    (bmp int64 [n], tile_row int32 [n], tile_col int32 [n], offset int32
+    [n+1]); one host synchronisation reads n."""
+    M = words.shape[0]
+    dev = words.device
+    T = ((M + 7) // 8) * ((K + 7) // 8)
+    bmp = torch.empty(max(T, 1), dtype=torch.int64, device=dev)
+    tr = torch.empty(max(T, 1), dtype=torch.int32, device=dev)
+    tc = torch.empty(max(T, 1), dtype=torch.int32, device=dev)
+    off = torch.empty(T + 1, dtype=torch.int32, device=dev)
+    n = torch.empty(1, dtype=torch.int64, device=dev)
+    ws = _ws("bsp_tiles8_workspace", M, K, device=dev)
+    call("bsp_rows_to_tiles8", _p(words), M, K, _p(bmp), _p(tr), _p(tc), _p(off), _p(n), _p(ws),
+         ws.numel(), _stream())
+    k = int(n.item())
+    return bmp[:k], tr[:k], tc[:k], off[: k + 1]
+
+
+def tiles8_to_rows(bmp, tile_row, tile_col, M, K, out=None):
+    """8x8 bitmap tiles -> packed rows [M, ceil(K/32)]."""
+    if out is None:
+        out = torch.empty((M, words_per_row(K)), dtype=torch.int32, device=bmp.device)
+    call("bsp_tiles8_to_rows", _p(bmp), _p(tile_row), _p(tile_col), bmp.numel(), M, K, _p(out), _stream())
+    return out
+
+
+def csr_to_tiled(row_ptr, col_idx, M, K, tile_rows, tile_cols, values=None):
+    """CSR -> tiled CSR of csr2tiledcsr (reference source/src/main.cu:499-588):
+    returns (tile_nnz_acc [T+1], tiled_offset [T, tile_rows+1], tiled_col
+    [nnz], tiled_values [nnz] or None)."""
+    dev = row_ptr.device
+    nnz = col_idx.numel()
+    T = ((M + tile_rows - 1) // tile_rows) * ((K + tile_cols - 1) // tile_cols)
+    acc = torch.empty(T + 1, dtype=torch.int32, device=dev)
+    toff = torch.empty((T, tile_rows + 1), dtype=torch.int32, device=dev)
+    tcol = torch.empty(max(nnz, 1), dtype=torch.int32, device=dev)
+    tval = torch.empty(max(nnz, 1), dtype=values.dtype, device=dev) if values is not None else None
+    ws = _ws("bsp_csr_to_tiled_workspace", M, K, nnz, tile_rows, tile_cols, device=dev)
+    call("bsp_csr_to_tiled", _p(row_ptr), _p(col_idx), _p(values) if values is not None else None,
+         values.element_size() if values is not None else 0, M, K, nnz, tile_rows, tile_cols, _p(acc), _p(toff),
+         _p(tcol), _p(tval) if tval is not None else None, _p(ws), ws.numel(), _stream())
+    return acc, toff, tcol[:nnz], (tval[:nnz] if tval is not None else None)
+
+
 class Batch:
     """Many independent C_i = A_i·B_i (16-bit B, shared N) in one persistent
     tensor-core launch.  ``problems``: list of (words, K, B, C) tensors; the

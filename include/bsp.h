@@ -273,10 +273,96 @@ int bsp_sddmm(const uint32_t* A_words, int64_t M, int64_t K, const void* G,
               float* dA, int64_t ldda, const bsp_plan* plan,
               bsp_stream_t stream);
 
+/* ======================================================================== */
+/* Output side and multi-bit operands                                       */
+/* ======================================================================== */
+
+/* Symbolic product of two bit matrices: C_words[M][ceil(N/32)] gets, for
+ * row i, the OR of B_words' row masks k over the set bits k of A's row i —
+ * the bit pattern of A·B's nonzeros when B (K×N) is itself a bitmap.  The
+ * symbolic half of pre_spgemm, source/src/transform.cuh:1028-1057; its
+ * first-fit grouping of the output rows (:1058-1157) is bsp_group_rows on
+ * C_words.  Both inputs and the output are LSB-first packed rows.          */
+int bsp_symbolic_rows(const uint32_t* A_words, int64_t M, int64_t K,
+                      const uint32_t* B_words, int64_t N, uint32_t* C_words,
+                      bsp_stream_t stream);
+
+/* Bit-plane product: C[M×N] (FP32, row stride ldc) = Σ_b w_b·(P_b·B) for the
+ * planes P_b (0 ≤ b < n_planes ≤ 8) of an M×K 8-bit matrix, packed as
+ * bsp_bitplanes writes them (planes[b][M][ceil(K/32)], LSB-first), with
+ * w_b = 2^b, except w = −2^(n_planes−1) for the top plane when
+ * is_signed != 0 (two's complement).  B is K×N of b_dtype ∈ {F32, F16,
+ * BF16}; every plane is summed in FP32 with a compensated (two-term) sum,
+ * then scaled by its exact power-of-two weight.  Replaces the bit-serial
+ * int8 product of spgemm_compute_1dthread_tcore_v3,
+ * source/src/transform.cuh:2199-2246, with the plane weights
+ * (1, 2, ..., 64, -128) of initialize_multiplicand, main.cu:895-910.      */
+int bsp_bitplane_spmm(const uint32_t* planes, int n_planes, int is_signed,
+                      int64_t M, int64_t K, const void* B, int b_dtype,
+                      int64_t ldb, int64_t N, float* C, int64_t ldc,
+                      bsp_stream_t stream);
+
+/* C = A·B for a dense int8 A (M×K, row stride lda): splits A into its 8
+ * bit planes in the workspace (bsp_spmm_i8_workspace bytes) and runs
+ * bsp_bitplane_spmm with the signed weights.  The whole path of the
+ * reference's multi-bit operand (layout_trans, backup/layout_trans.cu:75-97,
+ * then the bit-serial product above).                                     */
+int bsp_spmm_i8_workspace(int64_t M, int64_t K, size_t* bytes);
+int bsp_spmm_i8(const int8_t* A, int64_t M, int64_t K, int64_t lda,
+                const void* B, int b_dtype, int64_t ldb, int64_t N, float* C,
+                int64_t ldc, void* workspace, size_t workspace_bytes,
+                bsp_stream_t stream);
+
+/* ======================================================================== */
+/* Interchange formats                                                      */
+/* ======================================================================== */
+
+/* Packed rows -> 8x8 bitmap tiles (the tSparse format of coo2bmp_noTuple_d,
+ * source/src/main.cu:692-779, and find_tile_index, source/src/mm.h:83-104):
+ * the nonzero tiles in ascending tile_row*ceil(K/8)+tile_col order, each a
+ * uint64 with bit (r%8)*8 + c%8 for element (8*tile_row+r, 8*tile_col+c);
+ * offset[t] = Σ popcount of the tiles before t (offset[n] = nnz, where the
+ * values of tile t start in the reference's elems array).  Output arrays
+ * hold T = ceil(M/8)*ceil(K/8) entries (offset T+1); the first *n_tiles
+ * (device int64) are valid and offset[t] = nnz for t ≥ n.  Workspace:
+ * bsp_tiles8_workspace bytes.  Limit: M·K < 2^31.                         */
+int bsp_tiles8_workspace(int64_t M, int64_t K, size_t* bytes);
+int bsp_rows_to_tiles8(const uint32_t* words, int64_t M, int64_t K,
+                       uint64_t* bmp, int32_t* tile_row, int32_t* tile_col,
+                       int32_t* offset, int64_t* n_tiles, void* workspace,
+                       size_t workspace_bytes, bsp_stream_t stream);
+
+/* 8x8 bitmap tiles (n_tiles of them, any order, host count) -> packed rows
+ * (every word of words[M][ceil(K/32)] is written).  Tiles outside the
+ * matrix and bits past column K-1 are ignored.                             */
+int bsp_tiles8_to_rows(const uint64_t* bmp, const int32_t* tile_row,
+                       const int32_t* tile_col, int64_t n_tiles, int64_t M,
+                       int64_t K, uint32_t* words, bsp_stream_t stream);
+
+/* CSR (row_ptr[M+1], col_idx[nnz], optional values of value_bytes bytes
+ * each) -> tiled CSR of csr2tiledcsr, source/src/main.cu:499-588, with the
+ * tile shape tile_rows x tile_cols as parameters (TILE_HEIGHT x SPLIT_K
+ * there).  Tile t = ty*ceil(K/tile_cols)+tx holds its entries contiguously
+ * from tile_nnz_acc[t] (T+1 values, exclusive scan of the tiles' counts),
+ * rows in order and each row's entries in CSR order; tiled_col is the local
+ * column (col % tile_cols); tiled_offset[(tile_rows+1)*t + j] counts the
+ * tile's entries in its local rows before j.  Values are copied unchanged
+ * (the reference also cast them to its value type; cast before or after).
+ * Entries whose column is outside [0, K) are dropped.  Workspace:
+ * bsp_csr_to_tiled_workspace bytes.  Limits: nnz < 2^31, value_bytes ≤ 8. */
+int bsp_csr_to_tiled_workspace(int64_t M, int64_t K, int64_t nnz,
+                               int tile_rows, int tile_cols, size_t* bytes);
+int bsp_csr_to_tiled(const int32_t* row_ptr, const int32_t* col_idx,
+                     const void* values, int value_bytes, int64_t M,
+                     int64_t K, int64_t nnz, int tile_rows, int tile_cols,
+                     int32_t* tile_nnz_acc, int32_t* tiled_offset,
+                     int32_t* tiled_col, void* tiled_values, void* workspace,
+                     size_t workspace_bytes, bsp_stream_t stream);
+
 /* bsp_spmm without a workspace argument, for callers that may not allocate
  * device memory when they run the SpMM (plugin callbacks handed only
- * pointers, code inside CUDA stream capture, processes whose device memory
- * belongs to another allocator).  The prototype sums that bsp_spmm keeps in
+ * pointers, hot loops that must not call the allocator, processes whose
+ * device memory belongs to another allocator).  The prototype sums that bsp_spmm keeps in
  * the caller's workspace live in a static device array of 8 MiB inside the
  * library, held on every GPU that loads the library until the process exits.
  * Limit: bsp_spmm_workspace(plan, N) must be ≤ 8 MiB (≈ n_proto * N * 4

@@ -453,3 +453,90 @@ void orc_bitplane_spmm_f64(const int8_t* A, int64_t M, int64_t K,
         }
   }
 }
+
+/* 8x8 bitmap tiles, source/src/main.cu:692-779 (tile index = row/8 *
+ * ncols8 + col/8, position bit = (row%8)*8 + col%8, tiles reduced by OR in
+ * ascending tile index, offsets = exclusive scan of the popcounts).        */
+int64_t orc_rows_to_tiles8(const uint32_t* words, int64_t M, int64_t K,
+                           uint64_t* bmp, int32_t* tile_row, int32_t* tile_col,
+                           int32_t* offset) {
+  int64_t Kw = ceil32(K), Mt = (M + 7) / 8, Kt = (K + 7) / 8, n = 0, run = 0;
+  for (int64_t ty = 0; ty < Mt; ty++)
+    for (int64_t tx = 0; tx < Kt; tx++) {
+      uint64_t m = 0;
+      for (int64_t r = 0; r < 8; r++) {
+        int64_t row = ty * 8 + r;
+        if (row >= M) break;
+        for (int64_t c = 0; c < 8; c++) {
+          int64_t col = tx * 8 + c;
+          if (col >= K) break;
+          if ((words[row * Kw + col / 32] >> (col % 32)) & 1u) m |= 1ull << (r * 8 + c);
+        }
+      }
+      if (!m) continue;
+      bmp[n] = m;
+      tile_row[n] = (int32_t)ty;
+      tile_col[n] = (int32_t)tx;
+      offset[n] = (int32_t)run;
+      for (int b = 0; b < 64; b++) run += (m >> b) & 1u;
+      n++;
+    }
+  offset[n] = (int32_t)run;
+  return n;
+}
+
+void orc_tiles8_to_rows(const uint64_t* bmp, const int32_t* tile_row,
+                        const int32_t* tile_col, int64_t n, int64_t M,
+                        int64_t K, uint32_t* words) {
+  int64_t Kw = ceil32(K);
+  for (int64_t i = 0; i < M * Kw; i++) words[i] = 0;
+  for (int64_t t = 0; t < n; t++)
+    for (int b = 0; b < 64; b++) {
+      if (!((bmp[t] >> b) & 1u)) continue;
+      int64_t row = (int64_t)tile_row[t] * 8 + b / 8, col = (int64_t)tile_col[t] * 8 + b % 8;
+      if (row < M && col < K) words[row * Kw + col / 32] |= 1u << (col % 32);
+    }
+}
+
+/* csr2tiledcsr, source/src/main.cu:499-588: tile (ty, tx) of tile_rows x
+ * tile_cols, id ty*ceil(K/tile_cols)+tx; its entries in row order, each row's
+ * in CSR order; local column col % tile_cols; tile_nnz_acc = exclusive scan
+ * of the tiles' entry counts (T+1 values); tiled_offset[(tile_rows+1)*t + j]
+ * = entries of the tile in its local rows before j.                        */
+void orc_csr_to_tiled(const int32_t* row_ptr, const int32_t* col,
+                      const float* val, int64_t M, int64_t K, int tile_rows,
+                      int tile_cols, int32_t* tile_nnz_acc,
+                      int32_t* tiled_offset, int32_t* tiled_col,
+                      float* tiled_val) {
+  int64_t Mt = (M + tile_rows - 1) / tile_rows, Kt = (K + tile_cols - 1) / tile_cols, T = Mt * Kt;
+  int32_t* cnt = (int32_t*)calloc((size_t)T, sizeof(int32_t));
+  int32_t* fill = (int32_t*)calloc((size_t)T, sizeof(int32_t));
+  for (int64_t i = 0; i < M; i++)
+    for (int32_t j = row_ptr[i]; j < row_ptr[i + 1]; j++) cnt[(i / tile_rows) * Kt + col[j] / tile_cols]++;
+  int32_t run = 0;
+  for (int64_t t = 0; t < T; t++) {
+    tile_nnz_acc[t] = run;
+    run += cnt[t];
+  }
+  tile_nnz_acc[T] = run;
+  for (int64_t t = 0; t < T; t++) {
+    int64_t ty = t / Kt, tx = t % Kt;
+    int32_t r = 0;
+    for (int j = 0; j < tile_rows; j++) {
+      tiled_offset[(tile_rows + 1) * t + j] = r;
+      int64_t row = ty * tile_rows + j;
+      if (row < M)
+        for (int32_t e = row_ptr[row]; e < row_ptr[row + 1]; e++) r += (col[e] / tile_cols == tx);
+    }
+    tiled_offset[(tile_rows + 1) * t + tile_rows] = r;
+  }
+  for (int64_t i = 0; i < M; i++)
+    for (int32_t j = row_ptr[i]; j < row_ptr[i + 1]; j++) {
+      int64_t t = (i / tile_rows) * Kt + col[j] / tile_cols;
+      int32_t e = tile_nnz_acc[t] + fill[t]++;
+      tiled_col[e] = col[j] % tile_cols;
+      if (val && tiled_val) tiled_val[e] = val[j];
+    }
+  free(cnt);
+  free(fill);
+}

@@ -70,6 +70,25 @@ void orc_bitplane_spmm_f64(const int8_t* A, int64_t M, int64_t K,
                            int64_t lda, const float* B, int64_t ldb,
                            int64_t N, double* C, int64_t ldc);
 
+/* 8x8 bitmap tiles of packed LSB-first rows (tSparse format,
+ * coo2bmp_noTuple_d, source/src/main.cu:692-779, find_tile_index,
+ * source/src/mm.h:83-104): returns the number n of nonzero tiles, written in
+ * ascending tile_row*ceil(K/8)+tile_col order with bit (r%8)*8 + c%8, and
+ * offset[0..n] = exclusive scan of their popcounts.                        */
+int64_t orc_rows_to_tiles8(const uint32_t* words, int64_t M, int64_t K,
+                           uint64_t* bmp, int32_t* tile_row, int32_t* tile_col,
+                           int32_t* offset);
+void orc_tiles8_to_rows(const uint64_t* bmp, const int32_t* tile_row,
+                        const int32_t* tile_col, int64_t n, int64_t M,
+                        int64_t K, uint32_t* words);
+/* CSR -> tiled CSR of csr2tiledcsr, source/src/main.cu:499-588, with the
+ * tile shape as parameters (TILE_HEIGHT x SPLIT_K there).                  */
+void orc_csr_to_tiled(const int32_t* row_ptr, const int32_t* col,
+                      const float* val, int64_t M, int64_t K, int tile_rows,
+                      int tile_cols, int32_t* tile_nnz_acc,
+                      int32_t* tiled_offset, int32_t* tiled_col,
+                      float* tiled_val);
+
 #ifdef __cplusplus
 }
 #endif

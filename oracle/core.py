@@ -44,6 +44,9 @@ def lib():
             "orc_dense_check_sum_mt": (None, [_P, _P, _P, _I, _I, _I, _I, _I, _I]),
             "orc_symbolic_rows": (None, [_P, _I64, _I64, _P, _I64, _P]),
             "orc_bitplane_spmm_f64": (None, [_P, _I64, _I64, _I64, _P, _I64, _I64, _P, _I64]),
+            "orc_rows_to_tiles8": (_I64, [_P, _I64, _I64, _P, _P, _P, _P]),
+            "orc_tiles8_to_rows": (None, [_P, _P, _P, _I64, _I64, _I64, _P]),
+            "orc_csr_to_tiled": (None, [_P, _P, _P, _I64, _I64, _I, _I, _P, _P, _P, _P]),
         }
         for name, (res, args) in sigs.items():
             fn = getattr(L, name)
@@ -243,6 +246,43 @@ def bitplane_spmm_f64(A_i8, B):
     out = np.zeros((M, N), np.float64)
     lib().orc_bitplane_spmm_f64(_ptr(A), M, K, K, _ptr(B), N, N, _ptr(out), N)
     return out
+
+
+def rows_to_tiles8(words, M, K):
+    """-> (bmp uint64[n], tile_row int32[n], tile_col int32[n], offset int32[n+1])."""
+    words = _c(words, np.uint32)
+    T = ((M + 7) // 8) * ((K + 7) // 8)
+    bmp = np.zeros(T, np.uint64)
+    tr = np.zeros(T, np.int32)
+    tc = np.zeros(T, np.int32)
+    off = np.zeros(T + 1, np.int32)
+    n = int(lib().orc_rows_to_tiles8(_ptr(words), M, K, _ptr(bmp), _ptr(tr), _ptr(tc), _ptr(off)))
+    return bmp[:n], tr[:n], tc[:n], off[: n + 1]
+
+
+def tiles8_to_rows(bmp, tile_row, tile_col, M, K):
+    bmp = _c(bmp, np.uint64)
+    tr = _c(tile_row, np.int32)
+    tc = _c(tile_col, np.int32)
+    out = np.zeros((M, kw(K)), np.uint32)
+    lib().orc_tiles8_to_rows(_ptr(bmp), _ptr(tr), _ptr(tc), len(bmp), M, K, _ptr(out))
+    return out
+
+
+def csr_to_tiled(row_ptr, col, val, M, K, tile_rows, tile_cols):
+    """-> (tile_nnz_acc [T+1], tiled_offset [T, tile_rows+1], tiled_col [nnz], tiled_val [nnz])."""
+    rp = _c(row_ptr, np.int32)
+    cl = _c(col, np.int32)
+    vl = _c(val, np.float32)
+    T = ((M + tile_rows - 1) // tile_rows) * ((K + tile_cols - 1) // tile_cols)
+    nnz = len(cl)
+    acc = np.zeros(T + 1, np.int32)
+    toff = np.zeros((T, tile_rows + 1), np.int32)
+    tcol = np.zeros(max(nnz, 1), np.int32)
+    tval = np.zeros(max(nnz, 1), np.float32)
+    lib().orc_csr_to_tiled(_ptr(rp), _ptr(cl), _ptr(vl), M, K, tile_rows, tile_cols, _ptr(acc), _ptr(toff),
+                           _ptr(tcol), _ptr(tval))
+    return acc, toff, tcol[:nnz], tval[:nnz]
 
 
 def rel_errors(C, C64, Cabs=None):

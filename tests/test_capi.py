@@ -56,6 +56,18 @@ def test_argument_validation_without_gpu():
     assert L.bsp_spmm(fake, 4, 32, fake, 3, 8, 8, fake, 8, None, None, 0, None) == -4
     assert L.bsp_spmm(fake, 4, 32, fake, 0, 4, 8, fake, 8, None, None, 0, None) == -1
     assert L.bsp_spmm(fake, 4, 1 << 40, fake, 0, 8, 8, fake, 8, None, None, 0, None) == -8
+    # output side and multi-bit operands
+    assert L.bsp_symbolic_rows(fake, 4, 32, fake, -1, fake, None) == -1
+    assert L.bsp_symbolic_rows(fake, 4, 32, fake, 64, None, None) == -1
+    assert L.bsp_symbolic_rows(P(0x10002), 4, 32, fake, 64, fake, None) == -2
+    assert L.bsp_bitplane_spmm(fake, 0, 1, 4, 32, fake, 0, 8, 8, fake, 8, None) == -1
+    assert L.bsp_bitplane_spmm(fake, 9, 1, 4, 32, fake, 0, 8, 8, fake, 8, None) == -1
+    assert L.bsp_bitplane_spmm(fake, 8, 1, 4, 32, fake, 3, 8, 8, fake, 8, None) == -4
+    assert L.bsp_bitplane_spmm(fake, 8, 1, 4, 32, fake, 0, 4, 8, fake, 8, None) == -1
+    ws = C.c_size_t(0)
+    assert L.bsp_spmm_i8_workspace(3, 33, C.byref(ws)) == 0 and ws.value == 4 * 8 * 3 * 2 + 256
+    assert L.bsp_spmm_i8(fake, 3, 33, 40, fake, 0, 8, 8, fake, 8, None, 0, None) == -3
+    assert L.bsp_spmm_i8(fake, 3, 33, 32, fake, 0, 8, 8, fake, 8, fake, 1 << 20, None) == -1
     # plan handles
     assert L.bsp_plan_destroy(None) == 0
     assert L.bsp_plan_get_info(None, None) == -1

@@ -1,0 +1,91 @@
+"""Output side and multi-bit operands on the GPU: symbolic output masks and
+their first-fit grouping, bit-plane products and the int8 path, against the
+oracle (source/src/transform.cuh:1028-1157 and :2199-2246, main.cu:895-910)."""
+import numpy as np
+import pytest
+import torch
+
+import oracle as O
+from bitwise_spgemm_gb300 import ops
+from bitwise_spgemm_gb300 import workloads as W
+from gpu_util import dev, words_dev, words_host
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("M,K,N,pa,pb", [(300, 70, 90, 0.05, 0.1), (64, 4096, 5000, 0.002, 0.01),
+                                         (1000, 33, 31, 0.2, 0.05), (5, 32, 8192, 0.5, 0.001),
+                                         (128, 256, 1, 0.1, 0.5)])
+def test_symbolic_rows_match_oracle(M, K, N, pa, pb):
+    rng = np.random.default_rng(M * 7 + N)
+    A = rng.random((M, K)) < pa
+    A[M // 2] = False  # an empty row
+    Bm = rng.random((K, N)) < pb
+    a, b = W.pack_bits(A), W.pack_bits(Bm)
+    got = words_host(ops.symbolic_rows(words_dev(a), K, words_dev(b), N))
+    assert np.array_equal(got, O.symbolic_rows(a, K, b, N))
+    # the mask is the nonzero pattern of the integer product
+    prod = (A.astype(np.int64) @ Bm.astype(np.int64)) > 0
+    assert np.array_equal(got, W.pack_bits(prod))
+
+
+@pytest.mark.parametrize("TR,G", [(512, 2), (64, 4)])
+def test_output_grouping_of_symbolic_masks(TR, G):
+    # pre_spgemm's second half: first-fit grouping of the output rows
+    rng = np.random.default_rng(TR + G)
+    A = rng.random((1024, 256)) < 0.01
+    Bm = rng.random((256, 512)) < 0.01
+    a, b = W.pack_bits(A), W.pack_bits(Bm)
+    cw = ops.symbolic_rows(words_dev(a), 256, words_dev(b), 512)
+    g = ops.group_rows(cw, TR, G)
+    o = O.group_rows(O.symbolic_rows(a, 256, b, 512), TR, G)
+    for k in ("group_id", "group_row", "spill_cnt", "spill_nnz", "spill_rows"):
+        assert np.array_equal(g[k].cpu().numpy(), o[k]), k
+    assert np.array_equal(words_host(g["group_mask"]), o["group_mask"])
+
+
+def _int8(rng, M, K):
+    A = rng.integers(-128, 128, (M, K), dtype=np.int16).astype(np.int8)
+    A[0, : min(K, 4)] = [-128, 127, -1, 0][: min(K, 4)]
+    return A
+
+
+@pytest.mark.parametrize("M,K,N", [(200, 300, 256), (64, 1000, 96), (33, 65, 40), (8, 4096, 512)])
+def test_spmm_i8_integer_B_is_exact(M, K, N):
+    rng = np.random.default_rng(K)
+    A = _int8(rng, M, K)
+    B = rng.integers(-8, 9, (K, N)).astype(np.float32)
+    C = ops.spmm_i8(dev(A), dev(B)).cpu().numpy()
+    assert np.array_equal(C.astype(np.float64), A.astype(np.float64) @ B.astype(np.float64))
+
+
+@pytest.mark.parametrize("kind", ["f32", "bf16", "f16"])
+@pytest.mark.parametrize("M,K,N", [(128, 512, 128), (50, 77, 24), (17, 300, 33)])
+def test_bitplane_spmm_matches_oracle(kind, M, K, N):
+    rng = np.random.default_rng(M + K + N)
+    A = _int8(rng, M, K)
+    Bf = rng.standard_normal((K, N), dtype=np.float32)
+    tdt = {"f32": torch.float32, "bf16": torch.bfloat16, "f16": torch.float16}[kind]
+    Bt = dev(Bf).to(tdt)
+    Bq = Bt.float().cpu().numpy()  # the values the kernel reads
+    planes = ops.bitplanes(dev(A.view(np.uint8)), 8)
+    C = ops.bitplane_spmm(planes, K, Bt).cpu().numpy()
+    C64 = O.bitplane_spmm_f64(A, Bq)
+    Cabs = np.abs(A.astype(np.float64)) @ np.abs(Bq.astype(np.float64))
+    ms, _, mn = O.rel_errors(C, C64, Cabs)
+    assert ms <= 1e-5 and mn <= 1e-5, (ms, mn)
+    # the int8 entry point computes the same thing
+    C2 = ops.spmm_i8(dev(A), Bt).cpu().numpy()
+    assert np.array_equal(C, C2)
+
+
+def test_unsigned_planes_and_fewer_planes():
+    rng = np.random.default_rng(3)
+    U = rng.integers(0, 256, (96, 200), dtype=np.int16).astype(np.uint8)
+    B = rng.integers(-4, 5, (200, 64)).astype(np.float32)
+    planes = ops.bitplanes(dev(U), 8)
+    C = ops.bitplane_spmm(planes, 200, dev(B), signed=False).cpu().numpy()
+    assert np.array_equal(C.astype(np.float64), U.astype(np.float64) @ B.astype(np.float64))
+    # the low 3 planes only: values mod 8
+    C3 = ops.bitplane_spmm(planes[:3].contiguous(), 200, dev(B), signed=False).cpu().numpy()
+    assert np.array_equal(C3.astype(np.float64), (U % 8).astype(np.float64) @ B.astype(np.float64))

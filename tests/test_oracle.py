@@ -195,3 +195,66 @@ def test_live_reference_random_cases():
         Cr = R.uint8_spmm(R.uint8_layout_trans(A01), B)
         assert np.array_equal(Cr, O.spmm_f32(W.pack_bits(bits[:16]), K, B))
         assert R.check(A01.astype(np.float32), B, Cr)
+
+
+def _tiles8_numpy(A):
+    # find_tile_index (source/src/mm.h:83-104): tile = (r/8)*ncols8 + c/8,
+    # position bit = (r%8)*8 + c%8; tiles OR-reduced in ascending tile index
+    # and offsets = exclusive scan of popcounts (main.cu:692-779)
+    M, K = A.shape
+    ncols8 = (K + 7) // 8
+    tiles = {}
+    for r, c in zip(*np.nonzero(A)):
+        t = (r // 8) * ncols8 + c // 8
+        tiles[t] = tiles.get(t, 0) | (1 << int((r % 8) * 8 + c % 8))
+    keys = sorted(tiles)
+    bmp = np.array([tiles[t] for t in keys], np.uint64)
+    pc = [bin(tiles[t]).count("1") for t in keys]
+    off = np.concatenate([[0], np.cumsum(pc)]).astype(np.int32)
+    return bmp, np.array([t // ncols8 for t in keys], np.int32), np.array([t % ncols8 for t in keys], np.int32), off
+
+
+@pytest.mark.parametrize("M,K,p", [(37, 45, 0.1), (8, 8, 1.0), (64, 200, 0.02), (3, 5, 0.5)])
+def test_tiles8_oracle_matches_reference_formulas(M, K, p):
+    A = np.random.default_rng(M * K).random((M, K)) < p
+    w = W.pack_bits(A)
+    got = O.rows_to_tiles8(w, M, K)
+    ref = _tiles8_numpy(A)
+    for g, r in zip(got, ref):
+        assert np.array_equal(g, r)
+    assert np.array_equal(O.tiles8_to_rows(got[0], got[1], got[2], M, K), w)
+
+
+def _random_csr(rng, M, K, p, shuffle=False):
+    A = rng.random((M, K)) < p
+    row_ptr = np.concatenate([[0], np.cumsum(A.sum(1))]).astype(np.int32)
+    cols = [np.nonzero(A[i])[0] for i in range(M)]
+    if shuffle:
+        cols = [rng.permutation(c) for c in cols]
+    col = np.concatenate(cols).astype(np.int32) if cols else np.zeros(0, np.int32)
+    val = rng.standard_normal(len(col)).astype(np.float32)
+    return row_ptr, col, val
+
+
+@pytest.mark.parametrize("M,K,TR,TC,shuffle", [(100, 70, 16, 32, False), (37, 300, 8, 64, True),
+                                               (512, 2048, 512, 2048, False)])
+def test_csr_to_tiled_oracle_matches_csr2tiledcsr(M, K, TR, TC, shuffle):
+    # csr2tiledcsr (source/src/main.cu:499-588) restated with numpy: tiles in
+    # row-major order, rows in order, each row's entries in CSR order
+    rng = np.random.default_rng(M + K)
+    rp, col, val = _random_csr(rng, M, K, 0.05, shuffle)
+    acc, toff, tcol, tval = O.csr_to_tiled(rp, col, val, M, K, TR, TC)
+    Kt = (K + TC - 1) // TC
+    T = ((M + TR - 1) // TR) * Kt
+    buckets = [[] for _ in range(T)]
+    for i in range(M):
+        for j in range(rp[i], rp[i + 1]):
+            buckets[(i // TR) * Kt + col[j] // TC].append((i % TR, col[j] % TC, val[j]))
+    assert np.array_equal(acc, np.concatenate([[0], np.cumsum([len(b) for b in buckets])]))
+    flat = [e for b in buckets for e in b]
+    assert np.array_equal(tcol, np.array([e[1] for e in flat], np.int32).reshape(-1))
+    assert np.array_equal(tval, np.array([e[2] for e in flat], np.float32).reshape(-1))
+    for t, b in enumerate(buckets):
+        rows = np.array([e[0] for e in b], np.int64)
+        exp = [int((rows < j).sum()) for j in range(TR + 1)]
+        assert np.array_equal(toff[t], exp)
