@@ -43,7 +43,7 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=10)
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
+    p.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5", "f1", "f2", "f3"],
                    help="c2 (default): clustered FP32 8192x8192x512; c1: 1024x1024x256 "
                         "integer B; c3: block-structured 16384x16384x2048 BF16 (tensor cores); "
                         "c4: 512 batched problems, N=128 BF16; "
@@ -605,6 +605,167 @@ def run_fwd_bwd(args):
     plan.close()
 
 
+def _timed(fn, steps, warm):
+    import torch
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    cur = torch.cuda.current_stream()
+    e0.record(cur)
+    for _ in range(steps):
+        fn()
+    e1.record(cur)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def _cpu_rows(fn, M, rows0=64, budget=5.0):
+    """Seconds per full problem of a row-sliced oracle call, from the largest
+    row sample (doubling from rows0) that stays within the budget."""
+    rows = rows0
+    while True:
+        t0 = time.perf_counter()
+        fn(rows)
+        dt = time.perf_counter() - t0
+        if dt > budget / 4 or rows >= M:
+            return dt * M / rows, rows
+        rows = min(M, rows * 2)
+
+
+def run_next(args):
+    """The rows after the SpMM: f1 symbolic output masks + first-fit grouping
+    of the output rows, f2 bit-plane int8 product, f3 8x8 bitmap tiles and
+    tiled CSR.  One JSON line each; inputs resident, L2 flushed by the size of
+    the inputs where they exceed it (stated per workload)."""
+    import torch
+    import oracle as O
+    from bitwise_spgemm_gb300 import ops
+    from bitwise_spgemm_gb300 import workloads as W
+    ws, rank, local = dist_setup(args)
+    dev = torch.device("cuda", local)
+    hbm, hkind = peaks()
+    steps, warm = args.steps, max(args.warmup, 3)
+    sampler = ClockSampler(local) if rank == 0 else None
+    base = {"n_gpus": ws, "steps": steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "data": "synthetic (seeded numpy)"}
+    if args.config == "f1":
+        cfg = W.config_symbolic()
+        M, K, N = cfg["M"], cfg["K"], cfg["N"]
+        a = torch.from_numpy(cfg["a_words"].view(np.int32)).to(dev)
+        b = torch.from_numpy(cfg["b_words"].view(np.int32)).to(dev)
+        out = torch.empty(M, (N + 31) // 32, dtype=torch.int32, device=dev)
+        step = lambda: ops.symbolic_rows(a, K, b, N, out=out)
+        if sampler:
+            sampler.start()
+        barrier(ws)
+        ms = max_over_ranks(ws, _timed(step, steps, warm))
+        barrier(ws)
+        clocks = sampler.stop() if sampler else None
+        ms_group = _timed(lambda: ops.group_rows(out, 512, 2), 3, 1)
+        nnz = int(np.unpackbits(cfg["a_words"].view(np.uint8)).sum())
+        comp = 3 * M * ((N + 31) // 32) * 4
+        gather = nnz * ((N + 31) // 32) * 4
+        sec, rows = _cpu_rows(lambda r: O.symbolic_rows(cfg["a_words"][:r], K, cfg["b_words"], N), M)
+        line = dict(base, metric="symbolic output mask GB/s (A+B+C words / time)", value=comp / (ms * 1e-3) / 1e9,
+                    unit="GB/s", ms_per_step=ms, dtype="u32",
+                    config={"workload": cfg["name"], "M": M, "K": K, "N": N, "nnz_A": nnz,
+                            "l2": "B's words (8 MiB) stay in L2; the gathers are L2 reads"},
+                    gather_gbs=gather / (ms * 1e-3) / 1e9, grouping_ms=ms_group,
+                    roofline={"bound": "hbm", "achieved": comp / (ms * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
+                              "frac": comp / (ms * 1e-3) / 1e9 / hbm, "traffic": None, "peak_source": hkind},
+                    cpu_baseline={"value": comp / sec / 1e9, "unit": "GB/s", "cores": 1, "kind": "port",
+                                  "sample": "oracle symbolic pass on the first %d rows, scaled to %d" % (rows, M)},
+                    clocks=clocks)
+    elif args.config == "f2":
+        cfg = W.config_int8()
+        M, K, N = cfg["M"], cfg["K"], cfg["N"]
+        A = torch.from_numpy(cfg["A"]).to(dev)
+        B = torch.from_numpy(cfg["B"]).to(dev)
+        out = torch.empty(M, N, device=dev)
+        need = __import__("ctypes").c_size_t(0)
+        from bitwise_spgemm_gb300.capi import call
+        call("bsp_spmm_i8_workspace", M, K, __import__("ctypes").byref(need))
+        wsp = torch.empty(need.value, dtype=torch.uint8, device=dev)
+        step = lambda: ops.spmm_i8(A, B, out=out, workspace=wsp)
+        if sampler:
+            sampler.start()
+        barrier(ws)
+        ms = max_over_ranks(ws, _timed(step, steps, warm))
+        barrier(ws)
+        clocks = sampler.stop() if sampler else None
+        planes = ops.bitplanes(A.view(torch.uint8), 8)
+        ms_planes = _timed(lambda: ops.bitplanes(A.view(torch.uint8), 8, out=planes), 5, 2)
+        ms_prod = _timed(lambda: ops.bitplane_spmm(planes, K, B, out=out), 5, 2)
+        nnz = int((cfg["A"] != 0).sum())
+        plane_bits = int(np.unpackbits(planes.cpu().numpy().view(np.uint8)).sum())
+        comp = M * K + K * N * 4 + M * N * 4
+        sec, rows = _cpu_rows(lambda r: O.bitplane_spmm_f64(cfg["A"][:r], cfg["B"]), M, rows0=16)
+        line = dict(base, metric="int8 x dense product GB/s (A int8 + B + C / time)", value=comp / (ms * 1e-3) / 1e9,
+                    unit="GB/s", ms_per_step=ms, dtype="f32",
+                    config={"workload": cfg["name"], "M": M, "K": K, "N": N, "nnz_A": nnz, "plane_bits": plane_bits,
+                            "l2": "inputs (20 MiB) stay in L2"},
+                    effective_gflops=2.0 * nnz * N / (ms * 1e-3) / 1e9, bitplanes_ms=ms_planes, product_ms=ms_prod,
+                    gather_gbs=plane_bits * N * 4 / (ms_prod * 1e-3) / 1e9,
+                    roofline={"bound": "hbm", "achieved": comp / (ms * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
+                              "frac": comp / (ms * 1e-3) / 1e9 / hbm, "traffic": None, "peak_source": hkind},
+                    cpu_baseline={"value": comp / sec / 1e9, "unit": "GB/s", "cores": 1, "kind": "port",
+                                  "sample": "oracle bit-plane product (FP64) on the first %d rows, scaled to %d"
+                                  % (rows, M)},
+                    clocks=clocks)
+    else:
+        cfg = W.config3()
+        M, K = cfg["M"], cfg["K"]
+        words = torch.from_numpy(cfg["words"].view(np.int32)).to(dev)
+        Mt, Kt = (M + 7) // 8, (K + 7) // 8
+        T = Mt * Kt
+        bmp = torch.empty(T, dtype=torch.int64, device=dev)
+        tr = torch.empty(T, dtype=torch.int32, device=dev)
+        tc = torch.empty(T, dtype=torch.int32, device=dev)
+        off = torch.empty(T + 1, dtype=torch.int32, device=dev)
+        n = torch.empty(1, dtype=torch.int64, device=dev)
+        wsp = ops._ws("bsp_tiles8_workspace", M, K, device=dev)
+        from bitwise_spgemm_gb300.capi import call
+        p = ops._p
+        step = lambda: call("bsp_rows_to_tiles8", p(words), M, K, p(bmp), p(tr), p(tc), p(off), p(n), p(wsp),
+                            wsp.numel(), ops._stream())
+        if sampler:
+            sampler.start()
+        barrier(ws)
+        ms = max_over_ranks(ws, _timed(step, steps, warm))
+        barrier(ws)
+        clocks = sampler.stop() if sampler else None
+        ntiles = int(n.item())
+        back = torch.empty_like(words)
+        ms_back = _timed(lambda: ops.tiles8_to_rows(bmp[:ntiles], tr[:ntiles], tc[:ntiles], M, K, out=back), 5, 2)
+        comp = M * ((K + 31) // 32) * 4 + ntiles * 16 + 4
+        t0 = time.perf_counter()
+        O.rows_to_tiles8(cfg["words"], M, K)
+        cpu_tiles = time.perf_counter() - t0
+        c2 = W.config2()
+        rp, col = W.bits_to_csr(c2["words"], c2["M"], c2["K"])
+        val = np.random.default_rng(14).standard_normal(len(col)).astype(np.float32)
+        rp_d, col_d, val_d = (torch.from_numpy(x).to(dev) for x in (rp, col, val))
+        ms_csr = _timed(lambda: ops.csr_to_tiled(rp_d, col_d, c2["M"], c2["K"], 512, 2048, values=val_d), 5, 2)
+        t0 = time.perf_counter()
+        O.csr_to_tiled(rp, col, val, c2["M"], c2["K"], 512, 2048)
+        cpu_csr = time.perf_counter() - t0
+        line = dict(base, metric="packed rows -> 8x8 bitmap tiles GB/s (words read + tiles written / time)",
+                    value=comp / (ms * 1e-3) / 1e9, unit="GB/s", ms_per_step=ms, dtype="u64",
+                    config={"workload": "tiles8_" + cfg["name"], "M": M, "K": K, "n_tiles": ntiles,
+                            "l2": "32 MiB of words, 8.6 MB of tiles written"},
+                    tiles8_to_rows_ms=ms_back,
+                    csr_to_tiled={"workload": "csr_" + c2["name"] + "_tiles_512x2048", "nnz": int(len(col)),
+                                  "ms": ms_csr, "cpu_ms": cpu_csr * 1e3},
+                    roofline={"bound": "hbm", "achieved": comp / (ms * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
+                              "frac": comp / (ms * 1e-3) / 1e9 / hbm, "traffic": None, "peak_source": hkind},
+                    cpu_baseline={"value": comp / cpu_tiles / 1e9, "unit": "GB/s", "cores": 1, "kind": "port",
+                                  "sample": "oracle tile conversion of the full matrix"},
+                    clocks=clocks)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -613,6 +774,8 @@ def main():
         run_fwd_bwd(args)
     elif args.config == "c4":
         run_batched(args)
+    elif args.config in ("f1", "f2", "f3"):
+        run_next(args)
     elif args.config != "c2":
         run_other(args)
     else:

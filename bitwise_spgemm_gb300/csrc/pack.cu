@@ -169,6 +169,68 @@ __global__ void __launch_bounds__(256) k_bitplanes(const uint8_t* __restrict__ v
   }
 }
 
+// 8x8 bit-matrix transpose of a uint64 (byte i = row i): afterwards byte b,
+// bit i holds bit b of byte i (Hacker's Delight, section 7-3, transpose8).
+__device__ __forceinline__ uint64_t transpose8x8(uint64_t x) {
+  x = (x & 0xAA55AA55AA55AA55ull) | ((x & 0x00AA00AA00AA00AAull) << 7) | ((x >> 7) & 0x00AA00AA00AA00AAull);
+  x = (x & 0xCCCC3333CCCC3333ull) | ((x & 0x0000CCCC0000CCCCull) << 14) | ((x >> 14) & 0x0000CCCC0000CCCCull);
+  x = (x & 0xF0F0F0F00F0F0F0Full) | ((x & 0x00000000F0F0F0F0ull) << 28) | ((x >> 28) & 0x00000000F0F0F0F0ull);
+  return x;
+}
+
+// Bit planes from 16-byte rows: a warp takes 512 columns of a row (lane l
+// columns 16l..16l+15, one vector load), two 8x8 transposes give the lane's
+// 16-bit mask of every plane, and the even lane of each pair joins its mask
+// with its neighbour's into the 32-column word.  Rows must start 16-byte
+// aligned (ld % 16 == 0); the ragged end of a row is read byte by byte.
+__global__ void __launch_bounds__(256) k_bitplanes_v16(const uint8_t* __restrict__ v, int64_t M, int64_t K,
+                                                       int64_t ld, int planes, uint32_t* __restrict__ words,
+                                                       int64_t Kw, int msb) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int64_t nch = (K + 511) / 512;
+  for (int64_t t = warp; t < M * nch; t += nwarps) {
+    const int64_t r = t / nch, ch = t - r * nch;
+    const int64_t c = ch * 512 + lane * 16;
+    const uint8_t* p = v + r * ld + c;
+    uint64_t x0 = 0, x1 = 0;
+    if (c + 16 <= K) {
+      const uint4 q = __ldg(reinterpret_cast<const uint4*>(p));
+      x0 = (uint64_t)q.x | ((uint64_t)q.y << 32);
+      x1 = (uint64_t)q.z | ((uint64_t)q.w << 32);
+    } else {
+      for (int i = 0; i < 16; i++)
+        if (c + i < K) {
+          const uint64_t b = p[i];
+          if (i < 8) x0 |= b << (8 * i);
+          else x1 |= b << (8 * (i - 8));
+        }
+    }
+    x0 = transpose8x8(x0);
+    x1 = transpose8x8(x1);
+    // m[q] = 16-bit masks of planes 2q (low half) and 2q+1 (high half)
+    uint32_t m[4], n[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      m[q] = (uint32_t)((x0 >> (16 * q)) & 0xff) | ((uint32_t)((x1 >> (16 * q)) & 0xff) << 8) |
+             ((uint32_t)((x0 >> (16 * q + 8)) & 0xff) << 16) | ((uint32_t)((x1 >> (16 * q + 8)) & 0xff) << 24);
+      n[q] = __shfl_down_sync(kFull, m[q], 1);
+    }
+    const int64_t w = ch * 16 + (lane >> 1);
+    if ((lane & 1) == 0 && w < Kw) {
+#pragma unroll
+      for (int b = 0; b < 8; b++) {
+        if (b >= planes) break;
+        const int sh = 16 * (b & 1);
+        uint32_t word = ((m[b >> 1] >> sh) & 0xffffu) | (((n[b >> 1] >> sh) & 0xffffu) << 16);
+        if (msb) word = __brev(word);
+        words[((int64_t)b * M + r) * Kw + w] = word;
+      }
+    }
+  }
+}
+
 int grid_for(int64_t warps_needed) {
   const int64_t blocks = ceil_div(warps_needed, 8);
   const int64_t cap = (int64_t)num_sms() * 16;
@@ -236,7 +298,10 @@ int launch_unpack_rows(const uint32_t* words, int64_t M, int64_t K, void* dense,
 int launch_bitplanes(const uint8_t* v, int64_t M, int64_t K, int64_t ld, int planes,
                      uint32_t* words, int msb, cudaStream_t s) {
   const int64_t Kw = ceil_div(K, 32);
-  k_bitplanes<<<grid_for(M * Kw), 256, 0, s>>>(v, M, K, ld, planes, words, Kw, msb);
+  if (is_aligned(v, 16) && ld % 16 == 0)
+    k_bitplanes_v16<<<grid_for(M * ceil_div(K, 512)), 256, 0, s>>>(v, M, K, ld, planes, words, Kw, msb);
+  else
+    k_bitplanes<<<grid_for(M * Kw), 256, 0, s>>>(v, M, K, ld, planes, words, Kw, msb);
   BSP_LAUNCHED();
   return BSP_OK;
 }

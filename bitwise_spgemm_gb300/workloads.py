@@ -140,3 +140,32 @@ def config5(M=4096, K=4096, N=8192):
     G = np.random.default_rng(10).standard_normal((M, N), dtype=np.float32)
     return dict(M=M, K=K, N=N, words=pack_bits(A), X=f32_to_bf16_bits(X),
                 G=f32_to_bf16_bits(G))
+
+
+def config_symbolic(M=8192, K=8192, N=8192):
+    """Symbolic pass workload: A = the clustered 8192x8192 rows of config2
+    (seeds 2, 3), B a K x N bit matrix Bernoulli(0.002) (seed 11)."""
+    A, _, _ = clustered_bits(M, K)
+    Bm = bernoulli_bits(np.random.default_rng(11), K, N, 0.002)
+    return dict(name="symbolic_8192x8192x8192", M=M, K=K, N=N, a_words=pack_bits(A), b_words=pack_bits(Bm))
+
+
+def config_int8(M=4096, K=4096, N=256, density=0.05):
+    """Bit-plane product workload: A int8 M x K, nonzero w.p. 0.05 with values
+    uniform over the 255 nonzero int8 values (seed 12); B N(0,1) float32
+    (seed 13)."""
+    rng = np.random.default_rng(12)
+    mask = rng.random((M, K)) < density
+    vals = rng.integers(-128, 127, (M, K))  # -128..126, then 0..126 -> 1..127
+    A = np.where(mask, vals + (vals >= 0), 0).astype(np.int8)
+    B = np.random.default_rng(13).standard_normal((K, N), dtype=np.float32)
+    return dict(name="int8_bitplane_4096x4096x256_d0.05", M=M, K=K, N=N, A=A, B=B)
+
+
+def bits_to_csr(words, M, K):
+    """Packed rows -> (row_ptr int32 [M+1], col int32 [nnz]) on the host."""
+    dense = unpack_bits(words, K)
+    counts = dense.sum(1)
+    row_ptr = np.concatenate([[0], np.cumsum(counts)]).astype(np.int32)
+    col = np.nonzero(dense)[1].astype(np.int32)
+    return row_ptr, col

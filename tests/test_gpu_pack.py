@@ -75,3 +75,16 @@ def test_bitplanes_ragged():
     for planes in (1, 3, 8):
         got = ops.bitplanes(dev(v), planes=planes).cpu().numpy().view(np.uint32)
         assert np.array_equal(got, O.bitplanes(v, planes))
+
+
+@pytest.mark.parametrize("M,K,LD", [(64, 4096, 4096), (17, 1000, 1040), (5, 16, 16), (300, 512, 528),
+                                    (2, 530, 544)])
+def test_bitplanes_vector_path(M, K, LD):
+    # 16-byte aligned rows take the vector kernel (ragged row ends included)
+    rng = np.random.default_rng(M + K)
+    full = rng.integers(0, 256, (M, LD)).astype(np.uint8)
+    t = dev(full)[:, :K]
+    v = full[:, :K]
+    for planes, order in ((8, capi.LSB_FIRST), (3, capi.LSB_FIRST), (8, capi.MSB_FIRST)):
+        got = ops.bitplanes(t, planes=planes, bit_order=order).cpu().numpy().view(np.uint32)
+        assert np.array_equal(got, O.bitplanes(np.ascontiguousarray(v), planes, msb_first=order == capi.MSB_FIRST))
