@@ -699,6 +699,15 @@ def run_next(args):
         ms_prod = _timed(lambda: ops.bitplane_spmm(planes, K, B, out=out), 5, 2)
         nnz = int((cfg["A"] != 0).sum())
         plane_bits = int(np.unpackbits(planes.cpu().numpy().view(np.uint8)).sum())
+        # planes along K with bf16 B: one planned bitmap SpMM (tensor cores);
+        # the plane-weighted copies of B are stacked inside the timed step
+        mat = ops.Int8Matrix(A)
+        B16 = B.to(torch.bfloat16)
+        Bst = ops.stack_planes_b(B16, K)
+        out16 = torch.empty(M, N, device=dev)
+        ms_tc = _timed(lambda: mat.matmul(B16, out=out16, B_stacked=Bst), 10, 3)
+        tc_info = mat.plan.info()
+        mat.close()
         comp = M * K + K * N * 4 + M * N * 4
         sec, rows = _cpu_rows(lambda r: O.bitplane_spmm_f64(cfg["A"][:r], cfg["B"]), M, rows0=16)
         line = dict(base, metric="int8 x dense product GB/s (A int8 + B + C / time)", value=comp / (ms * 1e-3) / 1e9,
@@ -706,6 +715,8 @@ def run_next(args):
                     config={"workload": cfg["name"], "M": M, "K": K, "N": N, "nnz_A": nnz, "plane_bits": plane_bits,
                             "l2": "inputs (20 MiB) stay in L2"},
                     effective_gflops=2.0 * nnz * N / (ms * 1e-3) / 1e9, bitplanes_ms=ms_planes, product_ms=ms_prod,
+                    planes_along_k_bf16={"ms": ms_tc, "speedup_vs_fp32_bitplane": ms / ms_tc,
+                                         "occupied_tiles": tc_info["occ_tiles"], "plan_mode": tc_info["mode"]},
                     gather_gbs=plane_bits * N * 4 / (ms_prod * 1e-3) / 1e9,
                     roofline={"bound": "hbm", "achieved": comp / (ms * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
                               "frac": comp / (ms * 1e-3) / 1e9 / hbm, "traffic": None, "peak_source": hkind},

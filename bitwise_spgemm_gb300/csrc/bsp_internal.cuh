@@ -48,6 +48,10 @@ constexpr unsigned kFull = 0xffffffffu;
 __device__ __forceinline__ float to_f32(float x) { return x; }
 __device__ __forceinline__ float to_f32(__nv_bfloat16 x) { return __bfloat162float(x); }
 __device__ __forceinline__ float to_f32(__half x) { return __half2float(x); }
+template <typename T> __device__ __forceinline__ T from_f32(float x);
+template <> __device__ __forceinline__ float from_f32<float>(float x) { return x; }
+template <> __device__ __forceinline__ __nv_bfloat16 from_f32<__nv_bfloat16>(float x) { return __float2bfloat16_rn(x); }
+template <> __device__ __forceinline__ __half from_f32<__half>(float x) { return __float2half_rn(x); }
 
 // Internal launchers (defined in the .cu files, called from capi.cu).
 int launch_pack_rows(const void* dense, int dtype, int64_t M, int64_t K, int64_t ld,
@@ -58,8 +62,12 @@ int launch_transpose_bits(const uint32_t* words, int64_t M, int64_t K, uint32_t*
                           cudaStream_t s);
 int launch_unpack_rows(const uint32_t* words, int64_t M, int64_t K, void* dense, int dtype,
                        int64_t ld, int msb, cudaStream_t s);
+// rows_layout: words[M][planes][Kw] (planes of a row side by side) instead
+// of words[planes][M][Kw]
 int launch_bitplanes(const uint8_t* v, int64_t M, int64_t K, int64_t ld, int planes,
-                     uint32_t* words, int msb, cudaStream_t s);
+                     uint32_t* words, int msb, cudaStream_t s, int rows_layout = 0);
+int launch_stack_planes_b(const void* B, int bdt, int64_t ldb, int64_t K, int64_t N, int nplanes, int signed_top,
+                          void* out, int64_t ldo, cudaStream_t s);
 int launch_group_rows(const uint32_t* words, int64_t M, int64_t Kw, int tile_rows,
                       int max_groups, int32_t* group_id, uint32_t* group_mask,
                       int32_t* group_row, int32_t* spill_cnt, int32_t* spill_nnz,

@@ -366,6 +366,29 @@ int bsp_bitplane_spmm(const uint32_t* planes, int n_planes, int is_signed, int64
   return launch_bitplane_spmm(planes, n_planes, is_signed != 0, M, K, B, b_dtype, ldb, N, C, ldc, vec, s);
 }
 
+int bsp_bitplanes_rows(const uint8_t* values, int64_t M, int64_t K, int64_t ld, int n_planes, uint32_t* words,
+                       bsp_stream_t stream) {
+  BSP_TRY(check_dims(M, K));
+  if (n_planes < 1 || n_planes > 8 || ld < K) return BSP_ERR_INVALID_ARG;
+  if (ceil_div(K, 32) * n_planes > kMaxCols / 32) return BSP_ERR_CAPACITY;
+  if (M == 0 || K == 0) return BSP_OK;
+  if (!values || !words) return BSP_ERR_INVALID_ARG;
+  if (!is_aligned(words, 4)) return BSP_ERR_ALIGNMENT;
+  return launch_bitplanes(values, M, K, ld, n_planes, words, BSP_LSB_FIRST, (cudaStream_t)stream, 1);
+}
+
+int bsp_stack_planes_b(const void* B, int b_dtype, int64_t ldb, int64_t K, int64_t N, int n_planes, int is_signed,
+                       void* B_out, int64_t ld_out, bsp_stream_t stream) {
+  BSP_TRY(check_dims(K, N));
+  if (n_planes < 1 || n_planes > 8 || ldb < N || ld_out < N) return BSP_ERR_INVALID_ARG;
+  if (b_dtype != BSP_F32 && b_dtype != BSP_BF16 && b_dtype != BSP_F16) return BSP_ERR_UNSUPPORTED;
+  if (K == 0 || N == 0) return BSP_OK;
+  if (!B || !B_out) return BSP_ERR_INVALID_ARG;
+  const int esz = dtype_size(b_dtype);
+  if (!is_aligned(B, esz) || !is_aligned(B_out, esz)) return BSP_ERR_ALIGNMENT;
+  return launch_stack_planes_b(B, b_dtype, ldb, K, N, n_planes, is_signed != 0, B_out, ld_out, (cudaStream_t)stream);
+}
+
 int bsp_spmm_i8_workspace(int64_t M, int64_t K, size_t* bytes) {
   if (!bytes || M < 0 || K < 0) return BSP_ERR_INVALID_ARG;
   *bytes = sizeof(uint32_t) * 8 * (size_t)M * (size_t)ceil_div(K, 32) + 256;

@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(256) k_unpack_rows(const uint32_t* __restrict_
 __global__ void __launch_bounds__(256) k_bitplanes(const uint8_t* __restrict__ v, int64_t M,
                                                    int64_t K, int64_t ld, int planes,
                                                    uint32_t* __restrict__ words, int64_t Kw,
-                                                   int msb) {
+                                                   int msb, int rows_layout) {
   const int lane = threadIdx.x & 31;
   const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -165,7 +165,8 @@ __global__ void __launch_bounds__(256) k_bitplanes(const uint8_t* __restrict__ v
         if (lane == b) mine = m;
       }
     }
-    if (lane < planes) words[((int64_t)lane * M + r) * Kw + w] = mine;
+    if (lane < planes)
+      words[(rows_layout ? (r * planes + lane) : ((int64_t)lane * M + r)) * Kw + w] = mine;
   }
 }
 
@@ -185,7 +186,7 @@ __device__ __forceinline__ uint64_t transpose8x8(uint64_t x) {
 // aligned (ld % 16 == 0); the ragged end of a row is read byte by byte.
 __global__ void __launch_bounds__(256) k_bitplanes_v16(const uint8_t* __restrict__ v, int64_t M, int64_t K,
                                                        int64_t ld, int planes, uint32_t* __restrict__ words,
-                                                       int64_t Kw, int msb) {
+                                                       int64_t Kw, int msb, int rows_layout) {
   const int lane = threadIdx.x & 31;
   const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -225,7 +226,7 @@ __global__ void __launch_bounds__(256) k_bitplanes_v16(const uint8_t* __restrict
         const int sh = 16 * (b & 1);
         uint32_t word = ((m[b >> 1] >> sh) & 0xffffu) | (((n[b >> 1] >> sh) & 0xffffu) << 16);
         if (msb) word = __brev(word);
-        words[((int64_t)b * M + r) * Kw + w] = word;
+        words[(rows_layout ? (r * planes + b) : ((int64_t)b * M + r)) * Kw + w] = word;
       }
     }
   }
@@ -296,12 +297,13 @@ int launch_unpack_rows(const uint32_t* words, int64_t M, int64_t K, void* dense,
 }
 
 int launch_bitplanes(const uint8_t* v, int64_t M, int64_t K, int64_t ld, int planes,
-                     uint32_t* words, int msb, cudaStream_t s) {
+                     uint32_t* words, int msb, cudaStream_t s, int rows_layout) {
   const int64_t Kw = ceil_div(K, 32);
   if (is_aligned(v, 16) && ld % 16 == 0)
-    k_bitplanes_v16<<<grid_for(M * ceil_div(K, 512)), 256, 0, s>>>(v, M, K, ld, planes, words, Kw, msb);
+    k_bitplanes_v16<<<grid_for(M * ceil_div(K, 512)), 256, 0, s>>>(v, M, K, ld, planes, words, Kw, msb,
+                                                                  rows_layout);
   else
-    k_bitplanes<<<grid_for(M * Kw), 256, 0, s>>>(v, M, K, ld, planes, words, Kw, msb);
+    k_bitplanes<<<grid_for(M * Kw), 256, 0, s>>>(v, M, K, ld, planes, words, Kw, msb, rows_layout);
   BSP_LAUNCHED();
   return BSP_OK;
 }

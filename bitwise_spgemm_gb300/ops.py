@@ -256,6 +256,56 @@ def spmm_i8(A, B, out=None, workspace=None):
     return out
 
 
+def bitplanes_rows(values, planes=8, out=None):
+    """uint8/int8 [M, K] -> bit planes side by side per row, [M, planes *
+    ceil(K/32)] (a bitmap of planes * 32 * ceil(K/32) columns)."""
+    ld = _rowmajor(values, "values")
+    M, K = values.shape
+    if out is None:
+        out = torch.empty((M, planes * words_per_row(K)), dtype=torch.int32, device=values.device)
+    call("bsp_bitplanes_rows", _p(values), M, K, ld, planes, _p(out), _stream())
+    return out
+
+
+def stack_planes_b(B, K, planes=8, signed=True, out=None):
+    """[planes * 32 * ceil(K/32), N] blocks w_b * B (zero rows pad each block)."""
+    ldb = _rowmajor(B, "B")
+    N = B.shape[1]
+    Kp = words_per_row(K) * 32
+    if out is None:
+        out = torch.empty((planes * Kp, N), dtype=B.dtype, device=B.device)
+    call("bsp_stack_planes_b", _p(B), _DT[B.dtype], ldb, K, N, planes, int(signed), _p(out), out.stride(0),
+         _stream())
+    return out
+
+
+class Int8Matrix:
+    """An int8 matrix A [M, K] prepared for repeated products C = A·B: its 8
+    bit planes side by side per row (a bitmap with 8·32·ceil(K/32) columns)
+    and a plan of that bitmap.  ``matmul(B)`` stacks the plane-weighted
+    copies of B and runs the planned bitmap SpMM, which takes the tensor
+    cores for 16-bit B when the plan's cost model picks them — the
+    reference's bit-serial int8 product (transform.cuh:2199-2246) with the
+    2^b recombination folded into B."""
+
+    def __init__(self, A, **plan_kw):
+        if A.dtype != torch.int8 or A.dim() != 2:
+            raise ValueError("A must be a 2-D int8 tensor")
+        self.M, self.K = A.shape
+        self.Kc = 8 * words_per_row(self.K) * 32
+        self.words = bitplanes_rows(A.contiguous().view(torch.uint8), 8)
+        self.plan = Plan(self.words, self.Kc, **plan_kw)
+
+    def matmul(self, B, out=None, B_stacked=None):
+        if B.shape[0] != self.K:
+            raise ValueError("B must have K rows")
+        Bs = stack_planes_b(B, self.K, 8, True, out=B_stacked)
+        return spmm(self.words, self.Kc, Bs, plan=self.plan, out=out)
+
+    def close(self):
+        self.plan.close()
+
+
 def _ws(fn, *args, device):
     need = C.c_size_t(0)
     call(fn, *args, C.byref(need))

@@ -307,6 +307,22 @@ int bsp_bitplane_spmm(const uint32_t* planes, int n_planes, int is_signed,
  * bsp_bitplane_spmm with the signed weights.  The whole path of the
  * reference's multi-bit operand (layout_trans, backup/layout_trans.cu:75-97,
  * then the bit-serial product above).                                     */
+/* The same product as one bitmap SpMM with the planes laid along K, for a
+ * weight matrix A that is reused (plan it once with bsp_plan_create):
+ *   C = [P_0 | P_1 | ... | P_{n-1}] · [w_0·B; w_1·B; ...; w_{n-1}·B]
+ * bsp_bitplanes_rows writes A's planes side by side per row,
+ * words[M][n_planes*ceil(K/32)] (a bitmap with K' = n_planes*32*ceil(K/32)
+ * columns), and bsp_stack_planes_b writes the K'×N matrix of w_b·B blocks
+ * (rows K..32*ceil(K/32)-1 of every block are 0; scaling by a power of two
+ * is exact in every supported dtype).  bsp_spmm on the two, with a plan of
+ * the plane words, then runs on the tensor cores for 16-bit B when its cost
+ * model says so.                                                           */
+int bsp_bitplanes_rows(const uint8_t* values, int64_t M, int64_t K, int64_t ld,
+                       int n_planes, uint32_t* words, bsp_stream_t stream);
+int bsp_stack_planes_b(const void* B, int b_dtype, int64_t ldb, int64_t K,
+                       int64_t N, int n_planes, int is_signed, void* B_out,
+                       int64_t ld_out, bsp_stream_t stream);
+
 int bsp_spmm_i8_workspace(int64_t M, int64_t K, size_t* bytes);
 int bsp_spmm_i8(const int8_t* A, int64_t M, int64_t K, int64_t lda,
                 const void* B, int b_dtype, int64_t ldb, int64_t N, float* C,

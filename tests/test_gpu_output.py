@@ -89,3 +89,43 @@ def test_unsigned_planes_and_fewer_planes():
     # the low 3 planes only: values mod 8
     C3 = ops.bitplane_spmm(planes[:3].contiguous(), 200, dev(B), signed=False).cpu().numpy()
     assert np.array_equal(C3.astype(np.float64), (U % 8).astype(np.float64) @ B.astype(np.float64))
+
+
+@pytest.mark.parametrize("kind", ["bf16", "f16", "f32"])
+@pytest.mark.parametrize("M,K,N,d", [(512, 1024, 256, 0.05), (100, 77, 40, 0.3), (1024, 4096, 512, 0.02)])
+def test_int8_planes_along_k(kind, M, K, N, d, monkeypatch):
+    # C = [P_0 | ... | P_7] · [w_0 B; ...; w_7 B] through the planned bitmap
+    # SpMM, on the tensor cores (BSP_TC=1) and on the CUDA cores (BSP_TC=0)
+    rng = np.random.default_rng(M + K + N)
+    A = np.where(rng.random((M, K)) < d, rng.integers(-128, 128, (M, K)), 0).astype(np.int8)
+    A[0, :3] = [-128, 127, -1]
+    Bf = rng.standard_normal((K, N), dtype=np.float32)
+    tdt = {"f32": torch.float32, "bf16": torch.bfloat16, "f16": torch.float16}[kind]
+    Bt = dev(Bf).to(tdt)
+    Bq = Bt.float().cpu().numpy()
+    C64 = O.bitplane_spmm_f64(A, Bq)
+    # error scale of this form: sum_b |w_b| (P_b |B|) — the weighted plane
+    # terms it adds (an int8 -1 sets all 8 planes, |weights| summing to 255)
+    U = A.view(np.uint8)
+    W8 = sum((2.0 ** b) * ((U >> b) & 1).astype(np.float64) for b in range(8))
+    Cabs = W8 @ np.abs(Bq.astype(np.float64))
+    # the stacked B is exact: block b row k = w_b * B[k]
+    Bs = ops.stack_planes_b(Bt, K).float().cpu().numpy()
+    Kp = ((K + 31) // 32) * 32
+    for b, w in enumerate([1, 2, 4, 8, 16, 32, 64, -128]):
+        assert np.array_equal(Bs[b * Kp: b * Kp + K], w * Bq)
+        assert not Bs[b * Kp + K: (b + 1) * Kp].any()
+    # the plane rows hold the same bits as the plane-major layout
+    pr = ops.bitplanes_rows(dev(U)).cpu().numpy().view(np.uint32)
+    pm = O.bitplanes(U, 8)
+    assert np.array_equal(pr.reshape(M, 8, -1).transpose(1, 0, 2), pm)
+    tol = 1e-5 if kind == "f32" else 1e-3
+    for tc in ("1", "0"):
+        if kind == "f32" and tc == "1":
+            continue
+        monkeypatch.setenv("BSP_TC", tc)
+        mat = ops.Int8Matrix(dev(A))
+        C = mat.matmul(Bt).cpu().numpy()
+        mat.close()
+        ms, _, mn = O.rel_errors(C, C64, Cabs)
+        assert ms <= tol, (tc, ms, mn)
