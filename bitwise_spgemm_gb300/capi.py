@@ -77,6 +77,7 @@ SIGNATURES = {
     "bsp_symbolic_rows": [_P, _I64, _I64, _P, _I64, _P, _P],
     "bsp_bitplane_spmm": [_P, _I, _I, _I64, _I64, _P, _I, _I64, _I64, _P, _I64, _P],
     "bsp_spmm_i8_workspace": [_I64, _I64, C.POINTER(_SZ)],
+    "bsp_spmm_workspace_preferred": [_P, _I64, C.POINTER(_SZ)],
     "bsp_bitplanes_rows": [_P, _I64, _I64, _I64, _I, _P, _P],
     "bsp_stack_planes_b": [_P, _I, _I64, _I64, _I64, _I, _I, _P, _I64, _P],
     "bsp_spmm_i8": [_P, _I64, _I64, _I64, _P, _I, _I64, _I64, _P, _I64, _P, _SZ, _P],

@@ -260,6 +260,15 @@ int bsp_spmm_workspace(const bsp_plan* plan, int64_t N, size_t* bytes) {
   return BSP_OK;
 }
 
+int bsp_spmm_workspace_preferred(const bsp_plan* plan, int64_t N, size_t* bytes) {
+  BSP_TRY(bsp_spmm_workspace(plan, N, bytes));
+  if (plan) {
+    const size_t split = tc_split_bytes(plan->M, N, ceil_div(plan->K, 32));
+    if (split > *bytes) *bytes = split;
+  }
+  return BSP_OK;
+}
+
 int bsp_spmm(const uint32_t* A_words, int64_t M, int64_t K, const void* B, int b_dtype,
              int64_t ldb, int64_t N, float* C, int64_t ldc, const bsp_plan* plan, void* workspace,
              size_t workspace_bytes, bsp_stream_t stream) {
@@ -295,7 +304,7 @@ int bsp_spmm(const uint32_t* A_words, int64_t M, int64_t K, const void* B, int b
   // Tensor cores for 16-bit B when the occupied bit tiles make a dense
   // contraction cheaper than gathering B rows (BSP_TC=0/1 forces the choice).
   if (plan && vec && b_dtype != BSP_F32 && N % 8 == 0 && use_tensor_cores(plan, N, esz)) {
-    return launch_spmm_tc(a, plan->occ, s);
+    return launch_spmm_tc(a, plan->occ, s, workspace, workspace_bytes);
   }
   const bool proto = plan && plan->mode == BSP_PLAN_PROTO && vec;
   if (proto) {
@@ -508,7 +517,8 @@ int bsp_spmm_t(const uint32_t* A_words, int64_t M, int64_t K, const void* G, int
     const double tc = (double)plan->occT_tiles * 128.0 * 32.0 * (double)N * 2.0 / 1.2e15;
     const double cc = (double)plan->nnz * (double)N * (double)esz / 8e12;
     if (e ? e[0] == '1' : tc < cc)
-      return launch_spmm_t_tc(A_words, M, K, G, g_dtype, ldg, N, dX, lddx, plan->occT, s);
+      return launch_spmm_t_tc(A_words, M, K, G, g_dtype, ldg, N, dX, lddx, plan->occT, s, workspace,
+                              workspace_bytes);
   }
   // CUDA cores: transpose the bits into the workspace, then walk the rows of Aᵀ
   size_t need = 0;

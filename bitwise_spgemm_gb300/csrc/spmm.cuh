@@ -53,10 +53,15 @@ int launch_tile_occupancy(const uint32_t* A, int64_t M, int64_t K, uint32_t* occ
 // Occupancy of Aᵀ: [ceil(K/128)][tc_occupancy_t_words(M)], bit = 32-row tile
 int launch_tile_occupancy_t(const uint32_t* A, int64_t M, int64_t K, uint32_t* occT,
                             unsigned long long* count, cudaStream_t s);
-int launch_spmm_tc(const SpmmArgs& a, const uint32_t* occ, cudaStream_t s);
+// ws (optional): room for split-K partials; used when the output grid is
+// small and ws_bytes ≥ tc_split_bytes(...), else ignored.
+int launch_spmm_tc(const SpmmArgs& a, const uint32_t* occ, cudaStream_t s, void* ws = nullptr,
+                   size_t ws_bytes = 0);
+int tc_split_count(int64_t out_rows, int64_t out_cols, int64_t red_tiles);
+size_t tc_split_bytes(int64_t out_rows, int64_t out_cols, int64_t red_tiles);
 // dX[K][N] = Aᵀ·G on the tensor cores, Aᵀ read from A's row words
 int launch_spmm_t_tc(const uint32_t* A, int64_t M, int64_t K, const void* G, int gdt, int64_t ldg, int64_t N,
-                     float* dX, int64_t lddx, const uint32_t* occT, cudaStream_t s);
+                     float* dX, int64_t lddx, const uint32_t* occT, cudaStream_t s, void* ws = nullptr, size_t ws_bytes = 0);
 // dA[M][K] = (G·Xᵀ) at A's set bits, 0 elsewhere, on the tensor cores
 int launch_sddmm_tc(const uint32_t* A, int64_t M, int64_t K, const void* G, int64_t ldg, const void* X,
                     int64_t ldx, int dt, int64_t N, float* dA, int64_t ldda, cudaStream_t s);

@@ -88,7 +88,7 @@ struct __align__(1024) TcSmem {
   uint8_t a[kStages][kStageBytes];
   uint8_t b[kStages][kStageBytes];
   int list[kListMax];
-  int nlist, seen;
+  int nlist, seen, lo;
   uint64_t full[kStages];   // producer warps + the TMA transaction arrival
   uint64_t empty[kStages];  // tcgen05.commit of the stage's MMAs
   uint64_t done;
@@ -113,6 +113,10 @@ struct TcArgs {
   const uint32_t* occ;  // fwd / trans occupancy bitmap (unused by sddmm)
   int occ_words;
   int bdt;
+  // split-K (gridDim.z > 1): CTA z sums list slice z into part + z*part_stride
+  // (row stride ldp); a reduction kernel adds the slices into C
+  float* part;
+  int64_t ldp, part_stride;
 };
 
 // One kernel, three products (MODE):
@@ -160,13 +164,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
     const uint32_t* occ0 = a.occ + (int64_t)blockIdx.x * kHalves * a.occ_words;
     const bool has1 = (int)blockIdx.x * kHalves + 1 < nblk;
     int n = 0;
-    uint32_t any0 = 0, any1 = 0;
     for (int ow0 = 0; ow0 < a.occ_words; ow0 += 32) {
       const int ow = ow0 + lane;
       const uint32_t b0 = ow < a.occ_words ? __ldg(occ0 + ow) : 0u;
       const uint32_t b1 = (has1 && ow < a.occ_words) ? __ldg(occ0 + a.occ_words + ow) : 0u;
-      any0 |= b0;
-      any1 |= b1;
       uint32_t bits = b0 | b1;
       const int c = __popc(bits);
       int incl = c;
@@ -185,10 +186,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
       }
       n += __shfl_sync(kFull, incl, 31);
     }
-    const int seen = (__any_sync(kFull, any0 != 0u) ? 1 : 0) | (__any_sync(kFull, any1 != 0u) ? 2 : 0);
+    // this CTA's slice of the list (all of it without split-K) and the
+    // halves that slice touches
+    __syncwarp();
+    const int ntot = min(n, kListMax);
+    const int lo = (int)((int64_t)ntot * blockIdx.z / gridDim.z);
+    const int hi = (int)((int64_t)ntot * (blockIdx.z + 1) / gridDim.z);
+    uint32_t hs = 0;
+    for (int k = lo + lane; k < hi; k += 32) hs |= ((uint32_t)sm.list[k] >> 28) & 3u;
+    hs = __reduce_or_sync(kFull, hs);
     if (lane == 0) {
-      sm.nlist = min(n, kListMax);
-      sm.seen = seen;
+      sm.lo = lo;
+      sm.nlist = hi - lo;
+      sm.seen = (int)hs;
     }
   }
   // SDDMM: a block of A without set bits needs no product at all
@@ -202,6 +212,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
     if (tid == 0) {
       sm.nlist = any ? (int)((a.N + kSdK - 1) / kSdK) : 0;  // steps of kSdK columns of N
       sm.seen = any ? dense_halves : 0;
+      sm.lo = 0;
     }
   }
   ptx::tc_fence_before_sync();
@@ -209,6 +220,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
   ptx::tc_fence_after_sync();
   const uint32_t tmem = sm.tmem_addr;
   const int n = sm.nlist;
+  const int* lst = sm.list + sm.lo;  // this CTA's occupied tiles (fwd / trans)
   // stage i: list entries 2i and 2i+1 (fwd / trans) or N columns [64i, 64i+64) (SDDMM)
   const int nstages = MODE == kSddmm ? n : (n + kTilesPerStage - 1) / kTilesPerStage;
 
@@ -223,7 +235,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
       const int r = tid % kGroupThreads;
       auto load_word = [&](int k) -> uint32_t {
         if (k >= n) return 0u;
-        const int t = sm.list[k] & 0x0fffffff;
+        const int t = lst[k] & 0x0fffffff;
         if (MODE == kFwd) {
           const int64_t arow = row0 + r;
           return arow < a.M ? __ldg(a.A + arow * a.Kw + t) : 0u;
@@ -295,13 +307,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
         // B (fwd) / G (trans) rows t*32.. of the stage's tiles, columns col0 + 64*j
         const int k0 = kTilesPerStage * i;
         const bool two = k0 + 1 < n;
-        const int t0 = sm.list[k0] & 0x0fffffff;
+        const int t0 = lst[k0] & 0x0fffffff;
         ptx::mbar_arrive_expect_tx(&sm.full[s], (two ? 2 : 1) * kBTile);
 #pragma unroll
         for (int j = 0; j < kTcN / kBoxCols; j++)
           ptx::tma_load_2d_u32(bs + j * kBox, &mapB, (int)col0 + j * kBoxCols, t0 * kTcK, fb);
         if (two) {
-          const int t1 = sm.list[k0 + 1] & 0x0fffffff;
+          const int t1 = lst[k0 + 1] & 0x0fffffff;
 #pragma unroll
           for (int j = 0; j < kTcN / kBoxCols; j++)
             ptx::tma_load_2d_u32(bs + kBTile + j * kBox, &mapB, (int)col0 + j * kBoxCols, t1 * kTcK, fb);
@@ -326,8 +338,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
       int hv0 = dense_halves, hv1 = 0;
       if (MODE != kSddmm) {
         const int k0 = kTilesPerStage * i;
-        hv0 = (sm.list[k0] >> 28) & 3;
-        hv1 = k0 + 1 < n ? (sm.list[k0 + 1] >> 28) & 3 : 0;
+        hv0 = (lst[k0] >> 28) & 3;
+        hv1 = k0 + 1 < n ? (lst[k0 + 1] >> 28) & 3 : 0;
       }
       if (!ptx::mbar_wait(&sm.full[s], (i / kStages) & 1)) {
         atomicCAS(&g_tc_error, 0, 3);
@@ -384,7 +396,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
     }
     ptx::tc_fence_after_sync();
     const int64_t row = row0 + h * kTcM + q * 32 + lane;
-    float* crow = a.C + row * a.ldc + col0 + cg * (kTcN / 2);
+    float* crow = (gridDim.z > 1 ? a.part + (int64_t)blockIdx.z * a.part_stride + row * a.ldp
+                                 : a.C + row * a.ldc) + col0 + cg * (kTcN / 2);
     const bool live = row < out_rows && ok && !*(volatile int*)&sm.abort;
     const uint32_t* arow = a.A + row * a.Kw;
     const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * kTcN + cg * (kTcN / 2));
@@ -554,12 +567,66 @@ int launch_mode(const TcArgs& a, const CUtensorMap& ma, const CUtensorMap& mb, d
   return BSP_OK;
 }
 
+// C = Σ_z part[z] in ascending z (deterministic), four columns per thread
+// (the tensor-core path needs N % 8 == 0 and 16-byte aligned C rows).
+__global__ void __launch_bounds__(256) k_split_reduce(const float* __restrict__ part, int64_t ldp, int64_t stride,
+                                                      int splits, int64_t rows, int64_t cols, float* __restrict__ C,
+                                                      int64_t ldc) {
+  const int64_t q = cols / 4, total = rows * q;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = e / q, c = (e - r * q) * 4;
+    float4 acc = __ldg(reinterpret_cast<const float4*>(part + r * ldp + c));
+    for (int z = 1; z < splits; z++) {
+      const float4 v = __ldg(reinterpret_cast<const float4*>(part + z * stride + r * ldp + c));
+      acc.x += v.x;
+      acc.y += v.y;
+      acc.z += v.z;
+      acc.w += v.w;
+    }
+    *reinterpret_cast<float4*>(C + r * ldc + c) = acc;
+  }
+}
+
+}  // namespace
+
+// Split-K for the tensor-core products: when the output has fewer CTA tiles
+// than half the SMs, the reduction (list of occupied tiles) is cut into S
+// slices, up to 8 and at least 16 reduction tiles each, so that about one CTA
+// per SM runs; every slice's FP32 partial needs rows x round4(cols) floats.
+int tc_split_count(int64_t out_rows, int64_t out_cols, int64_t red_tiles) {
+  const int64_t tiles = ceil_div(out_rows, kCtaM) * ceil_div(out_cols, kTcN);
+  const int64_t sms = num_sms();
+  if (tiles == 0 || tiles * 2 > sms) return 1;
+  int64_t S = sms / tiles;
+  if (S > 8) S = 8;
+  if (S > red_tiles / 16) S = red_tiles / 16;
+  return S < 1 ? 1 : (int)S;
+}
+
+size_t tc_split_bytes(int64_t out_rows, int64_t out_cols, int64_t red_tiles) {
+  const int S = tc_split_count(out_rows, out_cols, red_tiles);
+  return S > 1 ? (size_t)S * (size_t)out_rows * (size_t)(ceil_div(out_cols, 4) * 4) * sizeof(float) + 256 : 0;
+}
+
+namespace {
+
 template <int MODE>
-int launch_tc(const TcArgs& a, cudaStream_t s) {
+int launch_tc(TcArgs a, cudaStream_t s, void* ws = nullptr, size_t ws_bytes = 0) {
   const int64_t rows = MODE == kTrans ? a.K : a.M;
   const int64_t cols = MODE == kSddmm ? a.K : a.N;
   if (rows == 0 || cols == 0) return BSP_OK;
-  const dim3 grid((unsigned)ceil_div(rows, kCtaM), (unsigned)ceil_div(cols, kTcN));
+  int splits = 1;
+  if (MODE != kSddmm && ws) {
+    const int64_t red_tiles = ceil_div(MODE == kFwd ? a.K : a.M, kTcK);
+    const int S = tc_split_count(rows, cols, red_tiles);
+    if (S > 1 && ws_bytes >= tc_split_bytes(rows, cols, red_tiles)) {
+      splits = S;
+      a.part = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(ws) + 255) & ~(uintptr_t)255);
+      a.ldp = ceil_div(cols, 4) * 4;
+      a.part_stride = rows * a.ldp;
+    }
+  }
+  const dim3 grid((unsigned)ceil_div(rows, kCtaM), (unsigned)ceil_div(cols, kTcN), (unsigned)splits);
   if (ceil_div(cols, kTcN) > 65535 || ceil_div(rows, kCtaM) > 0x7fffffff) return BSP_ERR_CAPACITY;
   if (a.N > INT32_MAX || a.M > INT32_MAX || a.K > INT32_MAX) return BSP_ERR_CAPACITY;
   // the tile list of a CTA holds every reduction tile (fwd: K, trans: M)
@@ -574,13 +641,21 @@ int launch_tc(const TcArgs& a, cudaStream_t s) {
     BSP_TRY(make_map(&mb, a.B, a.bdt, MODE == kFwd ? a.K : a.M, a.N, a.ldb, kBoxCols, kTcK,
                      CU_TENSOR_MAP_SWIZZLE_128B));
   }
-  if (a.bdt == BSP_BF16) return launch_mode<__nv_bfloat16, MODE>(a, ma, mb, grid, s);
-  if (a.bdt == BSP_F16) return launch_mode<__half, MODE>(a, ma, mb, grid, s);
-  return BSP_ERR_UNSUPPORTED;
+  if (a.bdt == BSP_BF16) BSP_TRY((launch_mode<__nv_bfloat16, MODE>(a, ma, mb, grid, s)));
+  else if (a.bdt == BSP_F16) BSP_TRY((launch_mode<__half, MODE>(a, ma, mb, grid, s)));
+  else return BSP_ERR_UNSUPPORTED;
+  if (splits > 1) {
+    const int64_t work = rows * (cols / 4);
+    const int64_t cap = (int64_t)num_sms() * 8;
+    k_split_reduce<<<(unsigned)(ceil_div(work, 256) < cap ? ceil_div(work, 256) : cap), 256, 0, s>>>(
+        a.part, a.ldp, a.part_stride, splits, rows, cols, a.C, a.ldc);
+    BSP_LAUNCHED();
+  }
+  return BSP_OK;
 }
 }  // namespace
 
-int launch_spmm_tc(const SpmmArgs& sa, const uint32_t* occ, cudaStream_t s) {
+int launch_spmm_tc(const SpmmArgs& sa, const uint32_t* occ, cudaStream_t s, void* ws, size_t ws_bytes) {
   TcArgs a = {};
   a.A = sa.A;
   a.M = sa.M;
@@ -594,11 +669,11 @@ int launch_spmm_tc(const SpmmArgs& sa, const uint32_t* occ, cudaStream_t s) {
   a.occ = occ;
   a.occ_words = tc_occupancy_words(sa.K);
   a.bdt = sa.bdt;
-  return launch_tc<kFwd>(a, s);
+  return launch_tc<kFwd>(a, s, ws, ws_bytes);
 }
 
 int launch_spmm_t_tc(const uint32_t* A, int64_t M, int64_t K, const void* G, int gdt, int64_t ldg, int64_t N,
-                     float* dX, int64_t lddx, const uint32_t* occT, cudaStream_t s) {
+                     float* dX, int64_t lddx, const uint32_t* occT, cudaStream_t s, void* ws, size_t ws_bytes) {
   TcArgs a = {};
   a.A = A;
   a.M = M;
@@ -612,7 +687,7 @@ int launch_spmm_t_tc(const uint32_t* A, int64_t M, int64_t K, const void* G, int
   a.occ = occT;
   a.occ_words = tc_occupancy_t_words(M);
   a.bdt = gdt;
-  return launch_tc<kTrans>(a, s);
+  return launch_tc<kTrans>(a, s, ws, ws_bytes);
 }
 
 int launch_sddmm_tc(const uint32_t* A, int64_t M, int64_t K, const void* G, int64_t ldg, const void* X,

@@ -135,9 +135,12 @@ class Plan:
         call("bsp_plan_get_info", self._h, C.byref(inf))
         return {f: getattr(inf, f) for f, _ in inf._fields_}
 
-    def workspace_bytes(self, N):
+    def workspace_bytes(self, N, preferred=True):
+        """Workspace for spmm with this plan; ``preferred`` includes room for
+        the tensor-core split of the reduction (bsp_spmm_workspace_preferred),
+        else the minimum (bsp_spmm_workspace)."""
         n = C.c_size_t()
-        call("bsp_spmm_workspace", self._h, N, C.byref(n))
+        call("bsp_spmm_workspace_preferred" if preferred else "bsp_spmm_workspace", self._h, N, C.byref(n))
         return n.value
 
     def close(self):

@@ -200,6 +200,14 @@ int bsp_plan_get_info(const bsp_plan* plan, bsp_plan_info* info);
 /* Device workspace (bytes) that bsp_spmm needs for this plan and N. */
 int bsp_spmm_workspace(const bsp_plan* plan, int64_t N, size_t* bytes);
 
+/* Workspace (bytes, ≥ the above) with which the tensor-core path may also
+ * split the reduction: when the output has fewer 256x256 tiles than half
+ * the SMs, up to 8 slices of the occupied K tiles run on separate CTAs and
+ * their FP32 partials (kept in the workspace) are added in a fixed order.
+ * A smaller workspace only turns the split off.  bsp_spmm_t uses its own
+ * workspace the same way when it is large enough.                        */
+int bsp_spmm_workspace_preferred(const bsp_plan* plan, int64_t N, size_t* bytes);
+
 /* C[M×N] (FP32, row stride ldc) = A·B, A given by its packed words and,
  * optionally, a plan built from the same words (NULL = walk every row's set
  * bits).  B is K×N of b_dtype ∈ {F32, F16, BF16}, row stride ldb elements;

@@ -101,3 +101,31 @@ def test_config3_full_size_row_sample():
     C64 = O.spmm_f64(words[rows], K, Bexact)
     mx, _, mxn = O.rel_errors(Cs, C64, O.spmm_abs_f64(words[rows], K, Bexact))
     assert mx <= TOL and mxn <= 1e-2
+
+
+@pytest.mark.parametrize("M,K,N,p", [(512, 8192, 256, 0.3), (300, 4096, 40, 0.1), (256, 16384, 512, 0.02)])
+def test_tc_split_k(force_tc, M, K, N, p):
+    # few output tiles and a long reduction: with the preferred workspace the
+    # occupied K tiles are split over several CTAs and the partials added in
+    # a fixed order; the minimum workspace keeps one CTA per output tile
+    rng = np.random.default_rng(M + K)
+    words = W.pack_bits(rng.random((M, K)) < p)
+    wd = words_dev(words)
+    plan = ops.Plan(wd, K)
+    assert plan.workspace_bytes(N) > plan.workspace_bytes(N, preferred=False)
+    Bi = rng.integers(-8, 9, (K, N)).astype(np.float32)
+    Bt, Bie = _b16(Bi, "bf16")
+    ref = O.spmm_f64(words, K, Bie)
+    C1 = ops.spmm(wd, K, Bt, plan=plan).cpu().numpy()  # split
+    ws0 = torch.empty(max(plan.workspace_bytes(N, preferred=False), 1), dtype=torch.uint8, device="cuda")
+    C0 = ops.spmm(wd, K, Bt, plan=plan, workspace=ws0).cpu().numpy()  # no split
+    assert capi.device_status() == 0
+    assert np.array_equal(C1.astype(np.float64), ref) and np.array_equal(C0.astype(np.float64), ref)
+    # N(0,1) B: both orders within the precision-form tolerance, split run to run identical
+    Bf = rng.standard_normal((K, N)).astype(np.float32)
+    B, Bexact = _b16(Bf, "bf16")
+    Ca = ops.spmm(wd, K, B, plan=plan).cpu().numpy()
+    Cb = ops.spmm(wd, K, B, plan=plan).cpu().numpy()
+    assert np.array_equal(Ca, Cb)
+    mx, _, _ = O.rel_errors(Ca, O.spmm_f64(words, K, Bexact), O.spmm_abs_f64(words, K, Bexact))
+    assert mx <= TOL, mx
