@@ -2,7 +2,8 @@
 
 Every ``csrc/*.cu`` is compiled by nvcc in parallel into ``_build/`` and
 linked into ``bitwise_spgemm_gb300/libbsp.so`` (CUDA runtime linked
-statically).  No cmake, one ``-gencode``; rebuilds only changed sources.
+statically), then the C++ harness ``harness/bsp_harness`` is linked against
+it.  No cmake, one ``-gencode``; rebuilds only changed sources.
 """
 import concurrent.futures as cf
 import glob
@@ -46,6 +47,23 @@ def _compile(src, force):
     return obj
 
 
+HARNESS_SRC = os.path.join(PKG, "harness", "bsp_harness.cpp")
+HARNESS = os.path.join(PKG, "harness", "bsp_harness")
+
+
+def build_harness(force=False):
+    """The C++ harness (replaces the reference's main(); C ABI only),
+    linked against the in-tree libbsp.so through an $ORIGIN rpath."""
+    newest = max(os.path.getmtime(p) for p in [HARNESS_SRC, LIB] + glob.glob(os.path.join(INCLUDE, "*.h")))
+    if not force and os.path.exists(HARNESS) and os.path.getmtime(HARNESS) >= newest:
+        return HARNESS
+    tmp = HARNESS + ".tmp%d" % os.getpid()
+    subprocess.check_call([nvcc(), "-O2", "-std=c++17", "-I", INCLUDE, HARNESS_SRC, "-o", tmp, "-L", PKG, "-lbsp",
+                           "-Xlinker", "-rpath,$ORIGIN/.."])
+    os.replace(tmp, HARNESS)
+    return HARNESS
+
+
 def build(force=False, jobs=None):
     os.makedirs(OBJ, exist_ok=True)
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
@@ -57,6 +75,7 @@ def build(force=False, jobs=None):
         tmp = LIB + ".tmp%d" % os.getpid()
         subprocess.check_call([nvcc()] + ARCH + ["-shared", "-o", tmp] + objs)
         os.replace(tmp, LIB)
+    build_harness(force)
     return LIB
 
 
