@@ -40,6 +40,10 @@ class PlanInfo(C.Structure):
                 ("direct_rows", C.c_int64), ("direct_nnz", C.c_int64), ("occ_tiles", C.c_int64)]
 
 
+class Schedule(C.Structure):
+    _fields_ = [("engine", C.c_int), ("proto_path", C.c_int), ("proto_variant", C.c_int), ("ms", C.c_float)]
+
+
 class Problem(C.Structure):
     _fields_ = [("A_words", C.c_void_p), ("M", C.c_int64), ("K", C.c_int64), ("B", C.c_void_p),
                 ("ldb", C.c_int64), ("C", C.c_void_p), ("ldc", C.c_int64)]
@@ -78,6 +82,11 @@ SIGNATURES = {
     "bsp_bitplane_spmm": [_P, _I, _I, _I64, _I64, _P, _I, _I64, _I64, _P, _I64, _P],
     "bsp_spmm_i8_workspace": [_I64, _I64, C.POINTER(_SZ)],
     "bsp_spmm_workspace_preferred": [_P, _I64, C.POINTER(_SZ)],
+    "bsp_tune": [_P, _I64, _I64, _P, _I, _I64, _I64, _P, _I64, _P, _P, _SZ, _P, C.POINTER(Schedule)],
+    "bsp_tune_cache_load": [C.c_char_p, C.POINTER(_I)],
+    "bsp_tune_cache_save": [C.c_char_p],
+    "bsp_tune_cache_clear": [],
+    "bsp_tune_cache_size": [C.POINTER(_I)],
     "bsp_bitplanes_rows": [_P, _I64, _I64, _I64, _I, _P, _P],
     "bsp_stack_planes_b": [_P, _I, _I64, _I64, _I64, _I, _I, _P, _I64, _P],
     "bsp_spmm_i8": [_P, _I64, _I64, _I64, _P, _I, _I64, _I64, _P, _I64, _P, _SZ, _P],

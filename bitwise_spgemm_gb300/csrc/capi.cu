@@ -8,6 +8,7 @@
 
 #include "bsp_internal.cuh"
 #include "plan.cuh"
+#include "tune.h"
 #include "spmm.cuh"
 
 namespace bsp {
@@ -251,6 +252,56 @@ static int proto_variant() {
   return v;
 }
 
+// Default schedule: the cost model for the engine (BSP_TC=0/1 forces it),
+// the measured default shape of the prototype kernels (BSP_PROTO_PATH /
+// BSP_PROTO_VARIANT override them).
+static TuneSched default_schedule(const bsp_plan* plan, int64_t N, int esz, bool tc_ok) {
+  TuneSched t;
+  t.engine = (tc_ok && use_tensor_cores(plan, N, esz)) ? 1 : 2;
+  t.proto_path = proto_path();
+  t.proto_variant = proto_variant();
+  return t;
+}
+
+// Runs the SpMM with a given schedule (arguments already validated).
+static int run_spmm(SpmmArgs a, const bsp_plan* plan, bool vec, const TuneSched& sc, void* workspace,
+                    size_t workspace_bytes, cudaStream_t s) {
+  // Tensor cores for 16-bit B when the occupied bit tiles make a dense
+  // contraction cheaper than gathering B rows.
+  if (sc.engine == 1) return launch_spmm_tc(a, plan->occ, s, workspace, workspace_bytes);
+  const int64_t N = a.N, K = a.K;
+  const bool proto = plan && plan->mode == BSP_PLAN_PROTO && vec;
+  if (proto) {
+    size_t need = 0;
+    bsp_spmm_workspace(plan, N, &need);
+    if (!workspace || workspace_bytes < need) return BSP_ERR_WORKSPACE;
+    a.row_cluster = plan->row_cluster;
+    a.delta_ptr = plan->delta_ptr;
+    a.delta_idx = plan->delta_idx;
+    a.cons = plan->cons;
+    a.n_proto = plan->n_proto;
+    a.P = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255));
+    a.ldp = proto_ldp(N);
+    a.n_delta = plan->delta_nnz;
+    if (K < (int64_t)1 << 30) {
+      // prototype sums, then clustered rows (register gathers, or slices
+      // staged by TMA bulk copies); rows without a cluster: walk A
+      BSP_TRY(launch_proto_sums(a, s));
+      if (sc.proto_path == 1) BSP_TRY(launch_spmm_proto_bulk(a, sc.proto_variant, s));
+      else BSP_TRY(launch_spmm_proto_regs(a, sc.proto_variant, s));
+      if (plan->direct_rows > 0) {
+        SpmmArgs d = a;
+        d.row_list = plan->direct_list;
+        d.n_list = plan->direct_rows;
+        BSP_TRY(launch_spmm_rows(d, false, vec, s));
+      }
+      return BSP_OK;
+    }
+    BSP_TRY(launch_proto_sums(a, s));
+  }
+  return launch_spmm_rows(a, proto, vec, s);
+}
+
 int bsp_spmm_workspace(const bsp_plan* plan, int64_t N, size_t* bytes) {
   if (!bytes || N < 0) return BSP_ERR_INVALID_ARG;
   *bytes = 0;
@@ -269,73 +320,136 @@ int bsp_spmm_workspace_preferred(const bsp_plan* plan, int64_t N, size_t* bytes)
   return BSP_OK;
 }
 
-int bsp_spmm(const uint32_t* A_words, int64_t M, int64_t K, const void* B, int b_dtype,
-             int64_t ldb, int64_t N, float* C, int64_t ldc, const bsp_plan* plan, void* workspace,
-             size_t workspace_bytes, bsp_stream_t stream) {
+// Validation and arguments shared by bsp_spmm and bsp_tune; kDone when the
+// product is empty (C already written or nothing to write).
+constexpr int kDone = 1;
+static int prepare_spmm(const uint32_t* A_words, int64_t M, int64_t K, const void* B, int b_dtype, int64_t ldb,
+                        int64_t N, float* C, int64_t ldc, const bsp_plan* plan, cudaStream_t s, SpmmArgs* a,
+                        bool* vec, bool* tc_ok, int* esz_out) {
   BSP_TRY(check_dims(M, K));
   if (N < 0 || N > kMaxCols) return BSP_ERR_INVALID_ARG;
   if (b_dtype != BSP_F32 && b_dtype != BSP_BF16 && b_dtype != BSP_F16) return BSP_ERR_UNSUPPORTED;
   if (ldb < N || ldc < N) return BSP_ERR_INVALID_ARG;
   if (plan && (plan->M != M || plan->K != K)) return BSP_ERR_INVALID_ARG;
   if (plan && plan->device != current_device()) return BSP_ERR_INVALID_ARG;
-  if (M == 0 || N == 0) return BSP_OK;
+  if (M == 0 || N == 0) return kDone;
   if (!C || (K > 0 && (!A_words || !B))) return BSP_ERR_INVALID_ARG;
   const int esz = dtype_size(b_dtype);
   if (!is_aligned(B, esz) || !is_aligned(C, 4) || !is_aligned(A_words, 4)) return BSP_ERR_ALIGNMENT;
-  const cudaStream_t s = (cudaStream_t)stream;
   if (K == 0) {  // C = 0
     BSP_CUDA(cudaMemset2DAsync(C, sizeof(float) * ldc, 0, sizeof(float) * N, M, s));
-    return BSP_OK;
+    return kDone;
   }
   const int vcols = b_dtype == BSP_F32 ? 4 : 8;
-  const bool vec = is_aligned(B, 16) && ((ldb * esz) % 16 == 0) && (N % vcols == 0) &&
-                   is_aligned(C, 16) && (ldc % 4 == 0);
-  SpmmArgs a = {};
-  a.A = A_words;
-  a.M = M;
-  a.K = K;
-  a.Kw = ceil_div(K, 32);
-  a.B = B;
-  a.bdt = b_dtype;
-  a.ldb = ldb;
-  a.N = N;
-  a.C = C;
-  a.ldc = ldc;
-  // Tensor cores for 16-bit B when the occupied bit tiles make a dense
-  // contraction cheaper than gathering B rows (BSP_TC=0/1 forces the choice).
-  if (plan && vec && b_dtype != BSP_F32 && N % 8 == 0 && use_tensor_cores(plan, N, esz)) {
-    return launch_spmm_tc(a, plan->occ, s, workspace, workspace_bytes);
+  *vec = is_aligned(B, 16) && ((ldb * esz) % 16 == 0) && (N % vcols == 0) && is_aligned(C, 16) && (ldc % 4 == 0);
+  *a = SpmmArgs{};
+  a->A = A_words;
+  a->M = M;
+  a->K = K;
+  a->Kw = ceil_div(K, 32);
+  a->B = B;
+  a->bdt = b_dtype;
+  a->ldb = ldb;
+  a->N = N;
+  a->C = C;
+  a->ldc = ldc;
+  *tc_ok = plan && *vec && b_dtype != BSP_F32 && N % 8 == 0 && plan->K <= tc_max_reduction();
+  *esz_out = esz;
+  return BSP_OK;
+}
+
+int bsp_spmm(const uint32_t* A_words, int64_t M, int64_t K, const void* B, int b_dtype,
+             int64_t ldb, int64_t N, float* C, int64_t ldc, const bsp_plan* plan, void* workspace,
+             size_t workspace_bytes, bsp_stream_t stream) {
+  const cudaStream_t s = (cudaStream_t)stream;
+  SpmmArgs a;
+  bool vec = false, tc_ok = false;
+  int esz = 4;
+  const int rc = prepare_spmm(A_words, M, K, B, b_dtype, ldb, N, C, ldc, plan, s, &a, &vec, &tc_ok, &esz);
+  if (rc != BSP_OK) return rc == kDone ? BSP_OK : rc;
+  // A measured schedule for this shape bucket (bsp_tune) replaces the cost
+  // model, unless the environment forces a choice.
+  TuneSched sc = default_schedule(plan, N, esz, tc_ok);
+  TuneSched tuned;
+  if (plan && !getenv("BSP_TC") && !getenv("BSP_PROTO_PATH") && !getenv("BSP_PROTO_VARIANT") &&
+      tune_lookup(plan, N, b_dtype, &tuned) && (tuned.engine == 2 || tc_ok))
+    sc = tuned;
+  return run_spmm(a, plan, vec, sc, workspace, workspace_bytes, s);
+}
+
+int bsp_tune(const uint32_t* A_words, int64_t M, int64_t K, const void* B, int b_dtype, int64_t ldb, int64_t N,
+             float* C, int64_t ldc, const bsp_plan* plan, void* workspace, size_t workspace_bytes,
+             bsp_stream_t stream, bsp_schedule* best) {
+  if (!plan || !best) return BSP_ERR_INVALID_ARG;
+  const cudaStream_t s = (cudaStream_t)stream;
+  SpmmArgs a;
+  bool vec = false, tc_ok = false;
+  int esz = 4;
+  const int rc = prepare_spmm(A_words, M, K, B, b_dtype, ldb, N, C, ldc, plan, s, &a, &vec, &tc_ok, &esz);
+  if (rc == kDone) return BSP_ERR_INVALID_ARG;  // nothing to time
+  BSP_TRY(rc);
+  // candidates: tensor cores; every prototype-kernel shape on both paths;
+  // the plain walk when the plan has no prototypes
+  TuneSched cand[1 + 7 + 8];
+  int nc = 0;
+  if (tc_ok) cand[nc++] = TuneSched{1, 0, 0, 0.0};
+  if (plan->mode == BSP_PLAN_PROTO && vec) {
+    for (int v = 0; v <= 6; v++) cand[nc++] = TuneSched{2, 0, v, 0.0};
+    for (int v = 0; v <= 7; v++) cand[nc++] = TuneSched{2, 1, v, 0.0};
+  } else {
+    cand[nc++] = TuneSched{2, 0, proto_variant(), 0.0};
   }
-  const bool proto = plan && plan->mode == BSP_PLAN_PROTO && vec;
-  if (proto) {
-    size_t need = 0;
-    bsp_spmm_workspace(plan, N, &need);
-    if (!workspace || workspace_bytes < need) return BSP_ERR_WORKSPACE;
-    a.row_cluster = plan->row_cluster;
-    a.delta_ptr = plan->delta_ptr;
-    a.delta_idx = plan->delta_idx;
-    a.cons = plan->cons;
-    a.n_proto = plan->n_proto;
-    a.P = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255));
-    a.ldp = proto_ldp(N);
-    a.n_delta = plan->delta_nnz;
-    if (K < (int64_t)1 << 30) {
-      // prototype sums, then clustered rows (register gathers, or slices
-      // staged by TMA bulk copies); rows without a cluster: walk A
-      BSP_TRY(launch_proto_sums(a, s));
-      if (proto_path() == 1) BSP_TRY(launch_spmm_proto_bulk(a, proto_variant(), s));
-      else BSP_TRY(launch_spmm_proto_regs(a, proto_variant(), s));
-      if (plan->direct_rows > 0) {
-        SpmmArgs d = a;
-        d.row_list = plan->direct_list;
-        d.n_list = plan->direct_rows;
-        BSP_TRY(launch_spmm_rows(d, false, vec, s));
-      }
-      return BSP_OK;
-    }
-    BSP_TRY(launch_proto_sums(a, s));
+  cudaEvent_t e0, e1;
+  BSP_CUDA(cudaEventCreate(&e0));
+  BSP_CUDA(cudaEventCreate(&e1));
+  int bi = -1;
+  int last = BSP_OK;
+  for (int c = 0; c < nc; c++) {
+    bool ok = true;
+    for (int r = 0; r < 2 && ok; r++) ok = (last = run_spmm(a, plan, vec, cand[c], workspace, workspace_bytes, s)) == BSP_OK;
+    if (!ok) continue;
+    const int reps = 5;
+    cudaEventRecord(e0, s);
+    for (int r = 0; r < reps && ok; r++) ok = (last = run_spmm(a, plan, vec, cand[c], workspace, workspace_bytes, s)) == BSP_OK;
+    cudaEventRecord(e1, s);
+    if (cudaEventSynchronize(e1) != cudaSuccess || !ok) continue;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cand[c].ms = ms / reps;
+    if (bi < 0 || cand[c].ms < cand[bi].ms) bi = c;
   }
-  return launch_spmm_rows(a, proto, vec, s);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (bi < 0) return last != BSP_OK ? last : BSP_ERR_INTERNAL;
+  // leave C holding the chosen schedule's result
+  BSP_TRY(run_spmm(a, plan, vec, cand[bi], workspace, workspace_bytes, s));
+  tune_store(tune_key(plan, N, b_dtype), cand[bi]);
+  best->engine = cand[bi].engine;
+  best->proto_path = cand[bi].proto_path;
+  best->proto_variant = cand[bi].proto_variant;
+  best->ms = (float)cand[bi].ms;
+  return BSP_OK;
+}
+
+int bsp_tune_cache_load(const char* path, int* entries) {
+  if (!path) return BSP_ERR_INVALID_ARG;
+  return tune_cache_load(path, entries);
+}
+
+int bsp_tune_cache_save(const char* path) {
+  if (!path) return BSP_ERR_INVALID_ARG;
+  return tune_cache_save(path);
+}
+
+int bsp_tune_cache_clear(void) {
+  tune_cache_clear();
+  return BSP_OK;
+}
+
+int bsp_tune_cache_size(int* entries) {
+  if (!entries) return BSP_ERR_INVALID_ARG;
+  *entries = tune_cache_size();
+  return BSP_OK;
 }
 
 int bsp_symbolic_rows(const uint32_t* A_words, int64_t M, int64_t K, const uint32_t* B_words, int64_t N,

@@ -208,6 +208,26 @@ def sddmm(words, M, K, G, X, plan=None, out=None):
     return out
 
 
+def tune(words, K, B, plan, out=None, workspace=None):
+    """Time every SpMM schedule for this plan and operands (bsp_tune), keep
+    the fastest in the library's per-shape-bucket cache and return it as a
+    dict (engine 1 = tensor cores, 2 = CUDA cores; prototype path and shape;
+    ms).  ``out`` ends holding the product."""
+    M = words.shape[0]
+    ldb = _rowmajor(B, "B")
+    N = B.shape[1]
+    if out is None:
+        out = torch.empty((M, N), dtype=torch.float32, device=B.device)
+    need = plan.workspace_bytes(N)
+    if workspace is None or workspace.numel() * workspace.element_size() < need:
+        workspace = torch.empty(max(need, 1), dtype=torch.uint8, device=B.device)
+    best = capi.Schedule()
+    call("bsp_tune", _p(words), M, K, _p(B), _DT[B.dtype], ldb, N, _p(out), out.stride(0), plan.handle,
+         _p(workspace), workspace.numel() * workspace.element_size(), _stream(), C.byref(best))
+    return {"engine": best.engine, "proto_path": best.proto_path, "proto_variant": best.proto_variant,
+            "ms": best.ms}
+
+
 def symbolic_rows(a_words, K, b_words, N, out=None):
     """Bit pattern of A·B for two bit matrices: row i of the result [M,
     ceil(N/32)] is the OR of B's row masks at A's set bits.  The symbolic

@@ -254,6 +254,42 @@ int bsp_batch_destroy(bsp_batch* batch);
 int bsp_batched_spmm(const bsp_batch* batch, bsp_stream_t stream);
 
 /* ======================================================================== */
+/* Autotuner                                                                */
+/* ======================================================================== */
+
+/* A measured SpMM schedule: engine 1 = tensor cores, 2 = CUDA cores; on the
+ * CUDA cores with a prototype plan, proto_path 0 = register gathers / 1 =
+ * TMA-staged slices and proto_variant = that kernel's shape; ms = its time. */
+typedef struct bsp_schedule {
+  int engine;
+  int proto_path;
+  int proto_variant;
+  float ms;
+} bsp_schedule;
+
+/* Times every candidate schedule of bsp_spmm for this plan and these
+ * operands (tensor cores when allowed; each prototype-kernel shape on both
+ * paths; 2 warm-up + 5 timed runs each, CUDA events on `stream`, which it
+ * synchronises), leaves C holding the fastest one's result, returns it in
+ * *best and caches it for the shape bucket (log2 of M, K, N; density in half
+ * octaves; dtype; plan mode).  bsp_spmm uses a cached schedule for its
+ * bucket unless BSP_TC, BSP_PROTO_PATH or BSP_PROTO_VARIANT force a choice.
+ * With BSP_TUNE_CACHE=<file> the cache is read from that JSON file at first
+ * use and rewritten (temporary file, then rename) after each new entry; a
+ * file that does not parse is ignored.  The reference fixed its tile shapes
+ * at compile time (source/src/common.h:15-35); no counterpart.            */
+int bsp_tune(const uint32_t* A_words, int64_t M, int64_t K, const void* B,
+             int b_dtype, int64_t ldb, int64_t N, float* C, int64_t ldc,
+             const bsp_plan* plan, void* workspace, size_t workspace_bytes,
+             bsp_stream_t stream, bsp_schedule* best);
+/* Replace the in-process cache by a file's entries (BSP_ERR_INVALID_ARG and
+ * no change if it does not parse), write it atomically, clear it, count it. */
+int bsp_tune_cache_load(const char* path, int* entries);
+int bsp_tune_cache_save(const char* path);
+int bsp_tune_cache_clear(void);
+int bsp_tune_cache_size(int* entries);
+
+/* ======================================================================== */
 /* Backward pass                                                            */
 /* ======================================================================== */
 

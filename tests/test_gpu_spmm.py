@@ -167,7 +167,7 @@ def test_plan_errors():
     wdp = words_dev(words)
     plan = ops.Plan(wdp, 1024, mode=capi.PLAN_PROTO)
     assert plan.info()["mode"] == capi.PLAN_PROTO
-    need = plan.workspace_bytes(64)
+    need = plan.workspace_bytes(64, preferred=False)  # the minimum: prototype sums
     ws = torch.empty(need - 300, dtype=torch.uint8, device="cuda")
     import ctypes as C
     Bt = torch.randn(1024, 64, device="cuda")

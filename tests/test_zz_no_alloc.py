@@ -68,7 +68,7 @@ def test_noalloc_rejects_prototype_sums_beyond_its_array():
     plan = ops.Plan(wd, K, mode=capi.PLAN_PROTO)
     n_proto = plan.info()["n_proto"]
     N = ((8 << 20) // (4 * max(n_proto, 1)) + 64) // 8 * 8   # prototype sums just past 8 MiB
-    assert plan.workspace_bytes(N) > (8 << 20)
+    assert plan.workspace_bytes(N, preferred=False) > (8 << 20)
     B = torch.zeros((K, N), device="cuda")
     out = torch.zeros((M, N), device="cuda")
     assert _noalloc(wd, M, K, B, out, plan) == -8  # BSP_ERR_CAPACITY, refused before any launch
