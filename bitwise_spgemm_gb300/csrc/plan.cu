@@ -30,6 +30,7 @@
 // Every step is order-independent or ordered by row index, so the plan is a
 // deterministic function of A.
 #include <climits>
+#include <mutex>
 #include <cstdlib>
 #include <new>
 
@@ -341,11 +342,49 @@ uint32_t pow2_at_least(int64_t n) {
   return p;
 }
 
+// Plan-build temporaries come from a library-owned, stream-ordered memory
+// pool per device that keeps its memory between builds (release threshold
+// = unlimited): no device-wide synchronisation on free, no remapping on the
+// next build.  Held until the process exits; bounded by the largest build.
+cudaMemPool_t temp_pool() {
+  static std::mutex mu;
+  static cudaMemPool_t pools[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> lk(mu);
+  if (!pools[dev]) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pool = nullptr;
+    if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) return nullptr;
+    uint64_t keep = ~0ull;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    pools[dev] = pool;
+  }
+  return pools[dev];
+}
+
 struct DevBuf {
   void* p = nullptr;
-  ~DevBuf() { if (p) cudaFree(p); }
-  int alloc(size_t bytes) {
-    const cudaError_t e = cudaMalloc(&p, bytes ? bytes : 16);
+  cudaStream_t s = nullptr;
+  bool pooled = false;
+  ~DevBuf() {
+    if (!p) return;
+    if (pooled) cudaFreeAsync(p, s);
+    else cudaFree(p);
+  }
+  int alloc(size_t bytes, cudaStream_t st) {
+    s = st;
+    cudaMemPool_t pool = temp_pool();
+    cudaError_t e;
+    if (pool) {
+      e = cudaMallocFromPoolAsync(&p, bytes ? bytes : 16, pool, st);
+      pooled = e == cudaSuccess;
+    } else {
+      e = cudaMalloc(&p, bytes ? bytes : 16);
+    }
     if (e != cudaSuccess) {
       p = nullptr;
       cuda_status(e);
@@ -356,6 +395,15 @@ struct DevBuf {
 };
 
 inline size_t al256(size_t b) { return (b + 255) & ~size_t(255); }
+
+// The plan's own storage, from the same pool (the plan is synchronised with
+// its stream before it is returned, so any stream may use it afterwards);
+// bsp_plan_destroy's cudaFree waits for the device and returns it there.
+cudaError_t plan_alloc(void** p, size_t bytes, cudaStream_t s) {
+  cudaMemPool_t pool = temp_pool();
+  if (pool && cudaMallocFromPoolAsync(p, bytes, pool, s) == cudaSuccess) return cudaSuccess;
+  return cudaMalloc(p, bytes);
+}
 
 }  // namespace
 
@@ -384,7 +432,7 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
   const size_t o_stats = take(sizeof(unsigned long long) * 8);
   const size_t o_dcnt = take(sizeof(int32_t) * M);
   DevBuf tmp;
-  BSP_TRY(tmp.alloc(off));
+  BSP_TRY(tmp.alloc(off, s));
   char* T = static_cast<char*>(tmp.p);
   uint32_t* sig = (uint32_t*)(T + o_sig);
   int32_t* nnz = (int32_t*)(T + o_nnz);
@@ -430,7 +478,7 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
   const size_t p_occ = ptake(sizeof(uint32_t) * ceil_div(M, 128) * tc_occupancy_words(K));
   const size_t p_occT = ptake(sizeof(uint32_t) * ceil_div(K, 128) * tc_occupancy_t_words(M));
   void* parena = nullptr;
-  BSP_CUDA(cudaMalloc(&parena, poff ? poff : 16));
+  BSP_CUDA(plan_alloc(&parena, poff ? poff : 16, s));
   plan->arena = parena;
   char* Pa = static_cast<char*>(parena);
   plan->row_cluster = (int32_t*)(Pa + p_cl);
@@ -438,9 +486,8 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
   plan->cons = (uint32_t*)(Pa + p_cons);
   plan->direct_list = (int32_t*)(Pa + p_dl);
   plan->occ = (uint32_t*)(Pa + p_occ);
-  BSP_TRY(launch_tile_occupancy(words, M, K, plan->occ, stats + 5, s));
   plan->occT = (uint32_t*)(Pa + p_occT);
-  BSP_TRY(launch_tile_occupancy_t(words, M, K, plan->occT, stats + 6, s));
+  BSP_TRY(launch_occupancy(words, M, K, plan->occ, plan->occT, stats + 5, stats + 6, s));
   plan->n_proto = ncl;
 
   if (ncl > 0) {
@@ -454,7 +501,7 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
     const size_t q_akeys = take2(sizeof(uint32_t) * asize * H);
     const size_t q_avals = take2(sizeof(int32_t) * asize * H);
     DevBuf t2;
-    BSP_TRY(t2.alloc(off2));
+    BSP_TRY(t2.alloc(off2, s));
     char* T2 = static_cast<char*>(t2.p);
     int32_t* counts = (int32_t*)(T2 + q_counts);
     int32_t* csize = (int32_t*)(T2 + q_csize);
@@ -516,7 +563,7 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
     BSP_LAUNCHED();
   }
   if (mode == BSP_PLAN_PROTO && plan->delta_nnz > 0) {
-    BSP_CUDA(cudaMalloc(&plan->delta_arena, sizeof(uint32_t) * plan->delta_nnz));
+    BSP_CUDA(plan_alloc(&plan->delta_arena, sizeof(uint32_t) * plan->delta_nnz, s));
     plan->delta_idx = (uint32_t*)plan->delta_arena;
     k_delta_fill<<<wgrid, 256, 0, s>>>(words, M, Kw, plan->cons, plan->row_cluster,
                                        plan->delta_ptr, plan->delta_idx);

@@ -48,11 +48,8 @@ int tc_occupancy_words(int64_t K);
 // a CTA lists its occupied 32-column tiles in shared memory.
 int64_t tc_max_reduction();
 int tc_occupancy_t_words(int64_t M);
-int launch_tile_occupancy(const uint32_t* A, int64_t M, int64_t K, uint32_t* occ,
-                          unsigned long long* count, cudaStream_t s);
-// Occupancy of Aᵀ: [ceil(K/128)][tc_occupancy_t_words(M)], bit = 32-row tile
-int launch_tile_occupancy_t(const uint32_t* A, int64_t M, int64_t K, uint32_t* occT,
-                            unsigned long long* count, cudaStream_t s);
+int launch_occupancy(const uint32_t* A, int64_t M, int64_t K, uint32_t* occ, uint32_t* occT,
+                     unsigned long long* count, unsigned long long* countT, cudaStream_t s);
 // ws (optional): room for split-K partials; used when the output grid is
 // small and ws_bytes ≥ tc_split_bytes(...), else ignored.
 int launch_spmm_tc(const SpmmArgs& a, const uint32_t* occ, cudaStream_t s, void* ws = nullptr,

@@ -443,49 +443,45 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
   }
 }
 
-// Occupancy of Aᵀ's tiles: warp per (128-column block of A, 32 consecutive
-// 32-row tiles); lane = row tile, OR of 32 rows x 4 words, one ballot.
-__global__ void __launch_bounds__(256) k_tile_occupancy_t(const uint32_t* __restrict__ A, int64_t M, int64_t Kw,
-                                                          int occ_words, int64_t nkb, uint32_t* __restrict__ occ,
-                                                          unsigned long long* __restrict__ count) {
-  const int lane = threadIdx.x & 31;
-  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  if (warp >= nkb * occ_words) return;
-  const int64_t kb = warp / occ_words;
-  const int ow = (int)(warp - kb * occ_words);
-  const int64_t it = (int64_t)ow * 32 + lane;
+// Both occupancy bitmaps in one pass over A's words.  A block of 4 warps
+// covers 128 rows x 32 word columns: thread (warp j, lane l) ORs the 32 rows
+// of row tile 4·blockIdx.y + j in word column 32·blockIdx.x + l (coalesced
+// across the lanes).  Forward: the OR of the 4 warps is the (128-row block,
+// K tile) bit, and the 32 lanes' bits are one occupancy word (one ballot).
+// Transposed: the OR of 4 neighbouring lanes is the (row tile, 128-column
+// block) bit of Aᵀ's bitmap, set with atomicOr (the bitmap is zeroed first;
+// a bit that was not yet set is counted).
+__global__ void __launch_bounds__(128) k_occupancy_both(const uint32_t* __restrict__ A, int64_t M, int64_t Kw,
+                                                        int ow, uint32_t* __restrict__ occ, int owt, int64_t nkb,
+                                                        uint32_t* __restrict__ occT, unsigned long long* count,
+                                                        unsigned long long* countT) {
+  __shared__ uint32_t s_or[4][32];
+  const int lane = threadIdx.x & 31, j = threadIdx.x >> 5;
+  const int64_t w = (int64_t)blockIdx.x * 32 + lane;
+  const int64_t rb = blockIdx.y, rt = rb * 4 + j;
   uint32_t acc = 0;
-  const int64_t r0 = it * kTcK, r1 = min(M, r0 + kTcK);
-  for (int64_t r = r0; r < r1; r++)
-    for (int64_t w = kb * 4; w < min(Kw, kb * 4 + 4); w++) acc |= __ldg(A + r * Kw + w);
-  const uint32_t m = __ballot_sync(kFull, acc != 0u);
-  if (lane == 0) {
-    occ[warp] = m;
-    if (count && m) atomicAdd(count, (unsigned long long)__popc(m));
+  if (w < Kw) {
+    const int64_t r0 = rt * 32, r1 = min(M, r0 + 32);
+    for (int64_t r = r0; r < r1; r++) acc |= __ldg(A + r * Kw + w);
   }
-}
-
-// Occupancy: warp per (128-row block, 32 consecutive K tiles); lane = K tile,
-// OR of the 128 rows' words, one ballot → occupancy word.
-__global__ void __launch_bounds__(256) k_tile_occupancy(const uint32_t* __restrict__ A, int64_t M, int64_t Kw,
-                                                        int occ_words, uint32_t* __restrict__ occ,
-                                                        unsigned long long* __restrict__ count) {
-  const int lane = threadIdx.x & 31;
-  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  const int64_t nrb = (M + kTcM - 1) / kTcM;
-  if (warp >= nrb * occ_words) return;
-  const int64_t rb = warp / occ_words;
-  const int ow = (int)(warp - rb * occ_words);
-  const int64_t kt = (int64_t)ow * 32 + lane;
-  uint32_t acc = 0;
-  if (kt < Kw) {
-    const int64_t r1 = min(M, (rb + 1) * kTcM);
-    for (int64_t r = rb * kTcM; r < r1; r++) acc |= __ldg(A + r * Kw + kt);
+  s_or[j][lane] = acc;
+  // transposed bitmap: 8 column blocks of 4 words per warp
+  uint32_t g = acc | __shfl_xor_sync(kFull, acc, 1);
+  g |= __shfl_xor_sync(kFull, g, 2);
+  const int64_t kb = w >> 2;
+  if ((lane & 3) == 0 && g != 0u && kb < nkb && rt * 32 < M) {
+    const uint32_t bit = 1u << (rt & 31);
+    const uint32_t old = atomicOr(occT + kb * owt + (rt >> 5), bit);
+    if (countT && !(old & bit)) atomicAdd(countT, 1ull);
   }
-  const uint32_t m = __ballot_sync(kFull, acc != 0u);
-  if (lane == 0) {
-    occ[warp] = m;
-    if (count && m) atomicAdd(count, (unsigned long long)__popc(m));
+  __syncthreads();
+  if (j == 0) {
+    const uint32_t v = s_or[0][lane] | s_or[1][lane] | s_or[2][lane] | s_or[3][lane];
+    const uint32_t m = __ballot_sync(kFull, v != 0u);
+    if (lane == 0) {
+      occ[rb * ow + blockIdx.x] = m;
+      if (count && m) atomicAdd(count, (unsigned long long)__popc(m));
+    }
   }
 }
 
@@ -495,23 +491,16 @@ int tc_occupancy_words(int64_t K) { return (int)ceil_div(ceil_div(K, 32), 32); }
 int64_t tc_max_reduction() { return (int64_t)kListMax * kTcK; }
 int tc_occupancy_t_words(int64_t M) { return (int)ceil_div(ceil_div(M, 32), 32); }
 
-int launch_tile_occupancy(const uint32_t* A, int64_t M, int64_t K, uint32_t* occ,
-                          unsigned long long* count, cudaStream_t s) {
-  const int ow = tc_occupancy_words(K);
-  const int64_t warps = ceil_div(M, kTcM) * ow;
-  if (warps == 0) return BSP_OK;
-  k_tile_occupancy<<<(unsigned)ceil_div(warps, 8), 256, 0, s>>>(A, M, ceil_div(K, 32), ow, occ, count);
-  BSP_LAUNCHED();
-  return BSP_OK;
-}
-
-int launch_tile_occupancy_t(const uint32_t* A, int64_t M, int64_t K, uint32_t* occT,
-                            unsigned long long* count, cudaStream_t s) {
-  const int ow = tc_occupancy_t_words(M);
-  const int64_t nkb = ceil_div(K, kTcM);
-  const int64_t warps = nkb * ow;
-  if (warps == 0) return BSP_OK;
-  k_tile_occupancy_t<<<(unsigned)ceil_div(warps, 8), 256, 0, s>>>(A, M, ceil_div(K, 32), ow, nkb, occT, count);
+int launch_occupancy(const uint32_t* A, int64_t M, int64_t K, uint32_t* occ, uint32_t* occT,
+                     unsigned long long* count, unsigned long long* countT, cudaStream_t s) {
+  const int64_t Kw = ceil_div(K, 32);
+  const int ow = tc_occupancy_words(K), owt = tc_occupancy_t_words(M);
+  const int64_t nkb = ceil_div(K, kTcM), nrb = ceil_div(M, kTcM);
+  if (M == 0 || K == 0) return BSP_OK;
+  if (nrb > 65535) return BSP_ERR_CAPACITY;
+  BSP_CUDA(cudaMemsetAsync(occT, 0, sizeof(uint32_t) * (size_t)nkb * owt, s));
+  k_occupancy_both<<<dim3((unsigned)ow, (unsigned)nrb), 128, 0, s>>>(A, M, Kw, ow, occ, owt, nkb, occT, count,
+                                                                      countT);
   BSP_LAUNCHED();
   return BSP_OK;
 }
