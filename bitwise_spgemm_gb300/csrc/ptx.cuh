@@ -165,6 +165,12 @@ __device__ __forceinline__ void tma_load_2d(void* dst_smem, const void* map, int
       : "memory");
 }
 
+// Acquire a tensor map that was written through the generic proxy (here: by
+// the host, into global memory) before TMA reads it.
+__device__ __forceinline__ void tensormap_acquire(const void* map) {
+  asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(map) : "memory");
+}
+
 // Shared-memory matrix descriptor (tcgen05), no swizzle: start address,
 // leading-dimension byte offset, stride byte offset (all >> 4), version 1.
 __device__ __forceinline__ uint64_t smem_desc_noswizzle_u32(uint32_t saddr, uint32_t lbo, uint32_t sbo) {

@@ -1,8 +1,26 @@
 // spmm.cuh — argument block and launchers of the CUDA-core SpMM kernels.
 #pragma once
+#include <cuda.h>
+
 #include "bsp_internal.cuh"
 
 namespace bsp {
+
+// One problem of the batched form on the tensor cores: B's tensor map (64x32
+// boxes, 128-byte swizzle; first, so the record keeps the map's alignment), A
+// and C.
+struct BatchProblemTc {
+  CUtensorMap map;
+  const uint32_t* A;
+  int64_t M, K, Kw;
+  float* C;
+  int64_t ldc;
+};
+// Tensor map of a batch problem's B [K][N] (row stride ldb elements).
+int make_batch_map(CUtensorMap* m, const void* B, int bdt, int64_t K, int64_t N, int64_t ldb);
+// Work item b = {problem, 256-row block, 256-column block, K tiles}: one CTA each.
+int launch_batched_tc(const BatchProblemTc* probs, const int4* items, int n_items, int64_t N, int bdt,
+                      cudaStream_t s);
 
 struct SpmmArgs {
   const uint32_t* A;  // packed rows [M][Kw], LSB-first

@@ -70,7 +70,7 @@ constexpr uint32_t kTmemCols = 512;       // two 128x256 FP32 accumulators
 using tc::kLbo;
 using tc::kSbo;
 using tc::kLayoutSw128;
-constexpr int kFwd = 0, kTrans = 1, kSddmm = 2;
+constexpr int kFwd = 0, kTrans = 1, kSddmm = 2, kBatch = 3;
 // B (fwd) / G (trans) tile: four TMA boxes of 64 columns x 32 reduction rows,
 // 128-byte swizzle, kBox bytes apart (the LBO); 8-row groups 1 KB apart (SBO).
 constexpr int kBoxCols = 64;
@@ -117,6 +117,9 @@ struct TcArgs {
   // (row stride ldp); a reduction kernel adds the slices into C
   float* part;
   int64_t ldp, part_stride;
+  // batched form (kBatch): CTA b runs work item b of the batch
+  const BatchProblemTc* bprobs;
+  const int4* items;  // {problem, 256-row block, 256-column block, K tiles}
 };
 
 // One kernel, three products (MODE):
@@ -136,10 +139,29 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
   TcSmem& sm = *reinterpret_cast<TcSmem*>(
       smem_raw + ((kSmemAlign - (ptx::smem_addr(smem_raw) & (kSmemAlign - 1))) & (kSmemAlign - 1)));
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int64_t row0 = (int64_t)blockIdx.x * kCtaM;  // output rows: M (fwd, sddmm) or K (trans)
-  const int64_t col0 = (int64_t)blockIdx.y * kTcN;   // output columns: N (fwd, trans) or K (sddmm)
-  const int64_t out_rows = MODE == kTrans ? a.K : a.M;
-  const int64_t out_cols = MODE == kSddmm ? a.K : a.N;
+  constexpr bool kFwdLike = MODE == kFwd || MODE == kBatch;
+  // the CTA's problem: the launch's (fwd / trans / sddmm) or its work item's (batch)
+  const uint32_t* gA = a.A;
+  int64_t gM = a.M, gK = a.K, gKw = a.Kw, gldc = a.ldc;
+  float* gC = a.C;
+  const void* bmap = &mapB;
+  int64_t row0 = (int64_t)blockIdx.x * kCtaM;  // output rows: M (fwd, sddmm, batch) or K (trans)
+  int64_t col0 = (int64_t)blockIdx.y * kTcN;   // output columns: N (fwd, trans, batch) or K (sddmm)
+  if (MODE == kBatch) {
+    const int4 it = a.items[blockIdx.x];
+    const BatchProblemTc& p = a.bprobs[it.x];
+    gA = p.A;
+    gM = p.M;
+    gK = p.K;
+    gKw = p.Kw;
+    gC = p.C;
+    gldc = p.ldc;
+    bmap = &p.map;
+    row0 = (int64_t)it.y * kCtaM;
+    col0 = (int64_t)it.z * kTcN;
+  }
+  const int64_t out_rows = MODE == kTrans ? gK : gM;
+  const int64_t out_cols = MODE == kSddmm ? gK : a.N;
   const int dense_halves = row0 + kTcM < out_rows ? 3 : 1;
 
   if (tid == 0) {
@@ -156,7 +178,18 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
     ptx::tmem_alloc(&sm.tmem_addr, kTmemCols);
     ptx::tmem_relinquish();
   }
-  if (MODE != kSddmm && warp == 0) {
+  if (MODE == kBatch && warp == 0) {
+    // every K tile (a batch has no occupancy plan), both halves that hold rows
+    const int ntot = (int)min(gKw, (int64_t)kListMax);
+    for (int k = lane; k < ntot; k += 32) sm.list[k] = k | (dense_halves << 28);
+    __syncwarp();
+    if (lane == 0) {
+      sm.lo = 0;
+      sm.nlist = ntot;
+      sm.seen = ntot > 0 ? dense_halves : 0;
+    }
+  }
+  if ((MODE == kFwd || MODE == kTrans) && warp == 0) {
     // List the occupied K tiles of the two 128-row blocks (ascending), with
     // the halves that have bits in each; the launcher guarantees that the
     // list fits (at most kListMax reduction tiles).
@@ -204,9 +237,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
   // SDDMM: a block of A without set bits needs no product at all
   if (MODE == kSddmm) {
     uint32_t acc = 0;
-    if (tid < kCtaM && row0 + tid < a.M) {
-      const uint32_t* arow = a.A + (row0 + tid) * a.Kw;
-      for (int64_t w = col0 / 32; w < min(a.Kw, (col0 + kTcN) / 32); w++) acc |= __ldg(arow + w);
+    if (tid < kCtaM && row0 + tid < gM) {
+      const uint32_t* arow = gA + (row0 + tid) * gKw;
+      for (int64_t w = col0 / 32; w < min(gKw, (col0 + kTcN) / 32); w++) acc |= __ldg(arow + w);
     }
     const int any = __syncthreads_or(acc != 0u);
     if (tid == 0) {
@@ -236,13 +269,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
       auto load_word = [&](int k) -> uint32_t {
         if (k >= n) return 0u;
         const int t = lst[k] & 0x0fffffff;
-        if (MODE == kFwd) {
+        if (kFwdLike) {
           const int64_t arow = row0 + r;
-          return arow < a.M ? __ldg(a.A + arow * a.Kw + t) : 0u;
+          return arow < gM ? __ldg(gA + arow * gKw + t) : 0u;
         }
         const int64_t arow = (int64_t)t * kTcK + (r & 31);
         const int64_t wcol = row0 / 32 + (r >> 5);
-        return (arow < a.M && wcol < a.Kw) ? __ldg(a.A + arow * a.Kw + wcol) : 0u;
+        return (arow < gM && wcol < gKw) ? __ldg(gA + arow * gKw + wcol) : 0u;
       };
       uint32_t wq[kWordAhead];
 #pragma unroll
@@ -264,7 +297,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
           uint8_t* at = sm.a[s] + u * kATile;
           uint4 e[4];
           tc::expand32_two(w0, e);
-          if (MODE == kFwd) {
+          if (kFwdLike) {
             // row r of the tile: half r/128 at 8 KB, then core matrices
             uint8_t* as = at + (r >> 3) * kSbo + (r & 7) * 16;
 #pragma unroll
@@ -289,6 +322,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
     // ---------------- TMA issuer ----------------
     // Shared-memory addresses are formed once; a stage adds its offset.
     const uint32_t a0 = ptx::smem_addr(sm.a[0]), b0 = ptx::smem_addr(sm.b[0]), f0 = ptx::smem_addr(&sm.full[0]);
+    if (MODE == kBatch) ptx::tensormap_acquire(bmap);  // written by the host into global memory
     for (int i = 0; i < nstages; i++) {
       const int s = i % kStages;
       if (i >= kStages && !ptx::mbar_wait(&sm.empty[s], ((i / kStages) - 1) & 1)) {
@@ -311,12 +345,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
         ptx::mbar_arrive_expect_tx(&sm.full[s], (two ? 2 : 1) * kBTile);
 #pragma unroll
         for (int j = 0; j < kTcN / kBoxCols; j++)
-          ptx::tma_load_2d_u32(bs + j * kBox, &mapB, (int)col0 + j * kBoxCols, t0 * kTcK, fb);
+          ptx::tma_load_2d_u32(bs + j * kBox, bmap, (int)col0 + j * kBoxCols, t0 * kTcK, fb);
         if (two) {
           const int t1 = lst[k0 + 1] & 0x0fffffff;
 #pragma unroll
           for (int j = 0; j < kTcN / kBoxCols; j++)
-            ptx::tma_load_2d_u32(bs + kBTile + j * kBox, &mapB, (int)col0 + j * kBoxCols, t1 * kTcK, fb);
+            ptx::tma_load_2d_u32(bs + kBTile + j * kBox, bmap, (int)col0 + j * kBoxCols, t1 * kTcK, fb);
         }
       }
     }
@@ -397,9 +431,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
     ptx::tc_fence_after_sync();
     const int64_t row = row0 + h * kTcM + q * 32 + lane;
     float* crow = (gridDim.z > 1 ? a.part + (int64_t)blockIdx.z * a.part_stride + row * a.ldp
-                                 : a.C + row * a.ldc) + col0 + cg * (kTcN / 2);
+                                 : gC + row * gldc) + col0 + cg * (kTcN / 2);
     const bool live = row < out_rows && ok && !*(volatile int*)&sm.abort;
-    const uint32_t* arow = a.A + row * a.Kw;
+    const uint32_t* arow = gA + row * gKw;
     const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * kTcN + cg * (kTcN / 2));
     for (int c8 = 0; c8 < kTcN / 16; c8 += 4) {
       uint32_t r[4][8];
@@ -695,6 +729,26 @@ int launch_sddmm_tc(const uint32_t* A, int64_t M, int64_t K, const void* G, int6
   a.ldc = ldda;
   a.bdt = dt;
   return launch_tc<kSddmm>(a, s);
+}
+
+int make_batch_map(CUtensorMap* m, const void* B, int bdt, int64_t K, int64_t N, int64_t ldb) {
+  return make_map(m, B, bdt, K, N, ldb, kBoxCols, kTcK, CU_TENSOR_MAP_SWIZZLE_128B);
+}
+
+int launch_batched_tc(const BatchProblemTc* probs, const int4* items, int n_items, int64_t N, int bdt,
+                      cudaStream_t s) {
+  if (n_items == 0 || N == 0) return BSP_OK;
+  TcArgs a = {};
+  a.N = N;
+  a.bdt = bdt;
+  a.bprobs = probs;
+  a.items = items;
+  CUtensorMap unused;
+  memset(&unused, 0, sizeof(unused));
+  const dim3 grid((unsigned)n_items, 1, 1);
+  if (bdt == BSP_BF16) return launch_mode<__nv_bfloat16, kBatch>(a, unused, unused, grid, s);
+  if (bdt == BSP_F16) return launch_mode<__half, kBatch>(a, unused, unused, grid, s);
+  return BSP_ERR_UNSUPPORTED;
 }
 
 int tc_device_error(int* out, bool clear) {

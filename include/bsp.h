@@ -241,16 +241,18 @@ typedef struct bsp_problem {
 typedef struct bsp_batch bsp_batch;
 
 /* Prepare a batch of n independent problems sharing N (multiple of 8) and a
- * 16-bit B type: uploads the descriptors and a device work queue of
- * (problem, 128-row block, column block) items sorted longest first;
- * synchronises the stream once.  The problems' buffers are referenced, not
- * copied — they must outlive the batch.  No reference counterpart (the
+ * 16-bit B type: encodes every problem's B tensor map and uploads them with
+ * a work list of (problem, 256-row block, 256-column block) items sorted
+ * longest reduction first; synchronises the stream once.  The problems'
+ * buffers are referenced, not copied — they must outlive the batch.  Limit:
+ * K ≤ 131072 per problem (BSP_ERR_CAPACITY).  No reference counterpart (the
  * reference runs one fixed-size problem per launch).                       */
 int bsp_batch_create(const bsp_problem* problems, int n, int64_t N,
                      int b_dtype, bsp_batch** batch, bsp_stream_t stream);
 int bsp_batch_destroy(bsp_batch* batch);
-/* Every problem of the batch in one persistent tensor-core launch (no host
- * synchronisation, no allocation: can be captured in a CUDA graph).       */
+/* Every problem of the batch in one tensor-core launch, one CTA per work
+ * item (no host synchronisation, no allocation: can be captured in a CUDA
+ * graph).                                                                  */
 int bsp_batched_spmm(const bsp_batch* batch, bsp_stream_t stream);
 
 /* ======================================================================== */
