@@ -96,9 +96,6 @@ struct __align__(1024) TcSmem {
   int abort;
 };
 
-__host__ __device__ constexpr uint32_t idesc_f16(uint32_t ab_type, uint32_t a_mn, uint32_t b_mn) {
-  return tc::idesc_f16(ab_type, a_mn, b_mn, kTcN, kTcM);
-}
 
 struct TcArgs {
   const uint32_t* A;  // bit matrix, packed rows [M][Kw]
@@ -162,6 +159,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
   }
   const int64_t out_rows = MODE == kTrans ? gK : gM;
   const int64_t out_cols = MODE == kSddmm ? gK : a.N;
+  // B boxes (64 columns) holding output columns of this CTA: a narrow last
+  // column tile loads, multiplies and stores only those (MMA N = 64·nbox)
+  const int nbox = MODE == kSddmm ? kTcN / kBoxCols
+                                  : (int)min((int64_t)(kTcN / kBoxCols), (out_cols - col0 + kBoxCols - 1) / kBoxCols);
   const int dense_halves = row0 + kTcM < out_rows ? 3 : 1;
 
   if (tid == 0) {
@@ -342,15 +343,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
         const int k0 = kTilesPerStage * i;
         const bool two = k0 + 1 < n;
         const int t0 = lst[k0] & 0x0fffffff;
-        ptx::mbar_arrive_expect_tx(&sm.full[s], (two ? 2 : 1) * kBTile);
+        ptx::mbar_arrive_expect_tx(&sm.full[s], (two ? 2 : 1) * nbox * kBox);
 #pragma unroll
         for (int j = 0; j < kTcN / kBoxCols; j++)
-          ptx::tma_load_2d_u32(bs + j * kBox, bmap, (int)col0 + j * kBoxCols, t0 * kTcK, fb);
+          if (j < nbox) ptx::tma_load_2d_u32(bs + j * kBox, bmap, (int)col0 + j * kBoxCols, t0 * kTcK, fb);
         if (two) {
           const int t1 = lst[k0 + 1] & 0x0fffffff;
 #pragma unroll
           for (int j = 0; j < kTcN / kBoxCols; j++)
-            ptx::tma_load_2d_u32(bs + kBTile + j * kBox, bmap, (int)col0 + j * kBoxCols, t1 * kTcK, fb);
+            if (j < nbox)
+              ptx::tma_load_2d_u32(bs + kBTile + j * kBox, bmap, (int)col0 + j * kBoxCols, t1 * kTcK, fb);
         }
       }
     }
@@ -359,7 +361,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
     // Descriptors of stage 0 are built once; every MMA adds a compile-time
     // offset (plus the stage's) to the 14-bit start-address field (>> 4).
     const uint32_t ab = std::is_same<BT, __nv_bfloat16>::value ? 1u : 0u;
-    const uint32_t idesc = idesc_f16(ab, MODE == kTrans ? 1u : 0u, MODE == kSddmm ? 0u : 1u);
+    const uint32_t idesc = tc::idesc_f16(ab, MODE == kTrans ? 1u : 0u, MODE == kSddmm ? 0u : 1u,
+                                         (uint32_t)(nbox * kBoxCols), kTcM);
     const uint32_t a0 = ptx::smem_addr(sm.a[0]), b0 = ptx::smem_addr(sm.b[0]);
     const uint64_t adesc = MODE == kSddmm ? ptx::smem_desc_noswizzle_u32(a0, 16, kSdSbo) | ((uint64_t)kLayoutSw128 << 61)
                                           : ptx::smem_desc_noswizzle_u32(a0, kLbo, kSbo);
@@ -435,7 +438,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
     const bool live = row < out_rows && ok && !*(volatile int*)&sm.abort;
     const uint32_t* arow = gA + row * gKw;
     const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * kTcN + cg * (kTcN / 2));
-    for (int c8 = 0; c8 < kTcN / 16; c8 += 4) {
+    // columns of this warp's half that hold output: up to 64·nbox of the tile
+    const int c8_end = (int)max(0, min(kTcN / 2, nbox * kBoxCols - cg * (kTcN / 2))) / 8;
+    for (int c8 = 0; c8 < c8_end; c8 += 4) {
       uint32_t r[4][8];
       if (have && ok) {
 #pragma unroll
