@@ -14,8 +14,9 @@
 //    row, with local columns, a local row pointer per tile and the exclusive
 //    scan of the tiles' entry counts.  Here a warp per CSR row ranks its
 //    entries within their (row, tile) runs (match_any + one atomicAdd per
-//    run, so CSR order is kept), a thread per tile turns the per-row counts
-//    into the local row pointer, and a second warp-per-row pass scatters.
+//    run, so CSR order is kept), a block scan per tile turns the per-row
+//    counts into the local row pointer, and a second warp-per-row pass
+//    scatters.
 #include "bsp_internal.cuh"
 
 namespace bsp {
@@ -106,23 +107,44 @@ __global__ void __launch_bounds__(256) k_csr_rank(const int32_t* __restrict__ ro
   }
 }
 
-// One thread per tile: the local row pointer (tile_rows+1 values) and the
-// tile's entry count.
+// One CTA per tile: the local row pointer (tile_rows+1 values) as a block
+// scan of the rows' counts in chunks of 256 rows, and the tile's entry count.
 __global__ void __launch_bounds__(256) k_tiled_offsets(const int32_t* __restrict__ cnt, int64_t M, int tr,
-                                                       int64_t Kt, int64_t T, int32_t* __restrict__ toff,
+                                                       int64_t Kt, int32_t* __restrict__ toff,
                                                        int32_t* __restrict__ tnnz) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= T) return;
+  __shared__ int32_t wsum[8];
+  const int64_t t = blockIdx.x;
   const int64_t ty = t / Kt, tx = t - ty * Kt;
-  int32_t run = 0;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   int32_t* o = toff + t * (tr + 1);
-  for (int j = 0; j < tr; j++) {
-    o[j] = run;
+  int32_t carry = 0;
+  for (int j0 = 0; j0 < tr; j0 += 256) {
+    const int j = j0 + threadIdx.x;
     const int64_t row = ty * tr + j;
-    if (row < M) run += __ldg(cnt + row * Kt + tx);
+    const int32_t v = (j < tr && row < M) ? __ldg(cnt + row * Kt + tx) : 0;
+    int32_t incl = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int32_t y = __shfl_up_sync(kFull, incl, d);
+      if (lane >= d) incl += y;
+    }
+    if (lane == 31) wsum[wid] = incl;
+    __syncthreads();
+    int32_t before = 0, total = 0;
+#pragma unroll
+    for (int w = 0; w < 8; w++) {
+      const int32_t x = wsum[w];
+      before += w < wid ? x : 0;
+      total += x;
+    }
+    if (j < tr) o[j] = carry + before + incl - v;
+    carry += total;
+    __syncthreads();
   }
-  o[tr] = run;
-  tnnz[t] = run;
+  if (threadIdx.x == 0) {
+    o[tr] = carry;
+    tnnz[t] = carry;
+  }
 }
 
 __global__ void __launch_bounds__(256) k_csr_fill(const int32_t* __restrict__ row_ptr,
@@ -213,7 +235,8 @@ int launch_csr_to_tiled(const int32_t* row_ptr, const int32_t* col, const void* 
   const unsigned gr = (unsigned)ceil_div(M, 8);
   k_csr_rank<<<gr, 256, 0, s>>>(row_ptr, col, M, K, tc, Kt, cnt, rank);
   BSP_LAUNCHED();
-  k_tiled_offsets<<<(unsigned)ceil_div(T, 256), 256, 0, s>>>(cnt, M, tr, Kt, T, toff, tnnz);
+  if (T > INT32_MAX) return BSP_ERR_CAPACITY;
+  k_tiled_offsets<<<(unsigned)T, 256, 0, s>>>(cnt, M, tr, Kt, toff, tnnz);
   BSP_LAUNCHED();
   BSP_TRY(launch_scan_i32(tnnz, T, acc, sws, s));
   k_csr_fill<<<gr, 256, 0, s>>>(row_ptr, col, static_cast<const uint8_t*>(val), vbytes, M, tr, tc, Kt, rank, acc,

@@ -158,18 +158,24 @@ int launch_planes_t(const PlaneArgs& a, bool vec, cudaStream_t s) {
 
 // B stacked for the planes-along-K form: row b*Kp + k of out is w_b·B[k]
 // (k < K) or 0 (K ≤ k < Kp, Kp = 32·ceil(K/32)).  A power-of-two factor
-// only changes the exponent, so the 16-bit values stay exact.
+// only changes the exponent, so the 16-bit values stay exact.  A CTA per
+// output row (grid-stride), its threads along the columns.
 template <typename BT>
 __global__ void __launch_bounds__(256) k_stack_planes_b(const BT* __restrict__ B, int64_t ldb, int64_t K,
                                                         int64_t Kp, int64_t N, int nplanes, int signed_top,
                                                         BT* __restrict__ out, int64_t ldo) {
-  const int64_t total = (int64_t)nplanes * Kp * N;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t rr = e / N, c = e - rr * N;
+  const int64_t rows = (int64_t)nplanes * Kp;
+  for (int64_t rr = blockIdx.x; rr < rows; rr += gridDim.x) {
     const int b = (int)(rr / Kp);
     const int64_t k = rr - (int64_t)b * Kp;
-    const float x = k < K ? to_f32(B[k * ldb + c]) * plane_weight(b, nplanes, signed_top) : 0.f;
-    out[rr * ldo + c] = from_f32<BT>(x);
+    const float w = plane_weight(b, nplanes, signed_top);
+    BT* o = out + rr * ldo;
+    if (k < K) {
+      const BT* src = B + k * ldb;
+      for (int64_t c = threadIdx.x; c < N; c += blockDim.x) o[c] = from_f32<BT>(to_f32(src[c]) * w);
+    } else {
+      for (int64_t c = threadIdx.x; c < N; c += blockDim.x) o[c] = from_f32<BT>(0.f);
+    }
   }
 }
 
@@ -180,8 +186,8 @@ int launch_stack_planes_b(const void* B, int bdt, int64_t ldb, int64_t K, int64_
   const int64_t Kp = ceil_div(K, 32) * 32;
   const int64_t total = (int64_t)nplanes * Kp * N;
   if (total == 0) return BSP_OK;
-  const int64_t cap = (int64_t)num_sms() * 32;
-  const unsigned grid = (unsigned)(ceil_div(total, 256) < cap ? ceil_div(total, 256) : cap);
+  const int64_t rows = (int64_t)nplanes * Kp, cap = (int64_t)num_sms() * 32;
+  const unsigned grid = (unsigned)(rows < cap ? rows : cap);
   if (bdt == BSP_F32)
     k_stack_planes_b<float><<<grid, 256, 0, s>>>((const float*)B, ldb, K, Kp, N, nplanes, signed_top, (float*)out, ldo);
   else if (bdt == BSP_BF16)
