@@ -82,6 +82,7 @@ SIGNATURES = {
     "bsp_bitplane_spmm": [_P, _I, _I, _I64, _I64, _P, _I, _I64, _I64, _P, _I64, _P],
     "bsp_spmm_i8_workspace": [_I64, _I64, C.POINTER(_SZ)],
     "bsp_spmm_workspace_preferred": [_P, _I64, C.POINTER(_SZ)],
+    "bsp_spmm_t_workspace_preferred": [_I64, _I64, _I64, C.POINTER(_SZ)],
     "bsp_tune": [_P, _I64, _I64, _P, _I, _I64, _I64, _P, _I64, _P, _P, _SZ, _P, C.POINTER(Schedule)],
     "bsp_tune_cache_load": [C.c_char_p, C.POINTER(_I)],
     "bsp_tune_cache_save": [C.c_char_p],

@@ -597,6 +597,14 @@ int bsp_csr_to_tiled(const int32_t* row_ptr, const int32_t* col_idx, const void*
                              tiled_offset, tiled_col, tiled_values, workspace, (cudaStream_t)stream);
 }
 
+int bsp_spmm_t_workspace_preferred(int64_t M, int64_t K, int64_t N, size_t* bytes) {
+  if (!bytes || M < 0 || K < 0 || N < 0) return BSP_ERR_INVALID_ARG;
+  BSP_TRY(bsp_spmm_t_workspace(M, K, bytes));
+  const size_t split = tc_split_bytes(K, N, ceil_div(M, 32));
+  if (split > *bytes) *bytes = split;
+  return BSP_OK;
+}
+
 int bsp_spmm_t_workspace(int64_t M, int64_t K, size_t* bytes) {
   if (!bytes || M < 0 || K < 0) return BSP_ERR_INVALID_ARG;
   *bytes = sizeof(uint32_t) * (size_t)K * (size_t)ceil_div(M, 32) + 256;

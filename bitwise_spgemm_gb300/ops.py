@@ -167,10 +167,13 @@ def spmm(words, K, B, plan=None, out=None, workspace=None):
     h = plan.handle if plan is not None else None
     ws_ptr, ws_n = None, 0
     if plan is not None:
-        need = plan.workspace_bytes(N)
-        if need:
-            if workspace is None or workspace.numel() * workspace.element_size() < need:
-                workspace = torch.empty(need, dtype=torch.uint8, device=B.device)
+        # a caller's workspace is used if it holds the minimum; without one,
+        # the preferred size (room for the tensor-core split) is allocated
+        have = workspace.numel() * workspace.element_size() if workspace is not None else 0
+        if workspace is None or have < plan.workspace_bytes(N, preferred=False):
+            need = plan.workspace_bytes(N)
+            workspace = torch.empty(max(need, 1), dtype=torch.uint8, device=B.device) if need else None
+        if workspace is not None:
             ws_ptr, ws_n = _p(workspace), workspace.numel() * workspace.element_size()
     call("bsp_spmm", _p(words), M, K, _p(B), _DT[B.dtype], ldb, N, _p(out), ldc, h, ws_ptr, ws_n,
          _stream())
@@ -183,10 +186,12 @@ def spmm_t(words, M, K, G, plan=None, out=None, workspace=None):
     N = G.shape[1]
     if out is None:
         out = torch.empty((K, N), dtype=torch.float32, device=G.device)
-    n = C.c_size_t()
-    call("bsp_spmm_t_workspace", M, K, C.byref(n))
-    if workspace is None or workspace.numel() * workspace.element_size() < n.value:
-        workspace = torch.empty(n.value, dtype=torch.uint8, device=G.device)
+    n_min, n_pref = C.c_size_t(), C.c_size_t()
+    call("bsp_spmm_t_workspace", M, K, C.byref(n_min))
+    call("bsp_spmm_t_workspace_preferred", M, K, N, C.byref(n_pref))
+    # a caller's workspace is used if it holds the minimum; else the preferred size
+    if workspace is None or workspace.numel() * workspace.element_size() < n_min.value:
+        workspace = torch.empty(n_pref.value, dtype=torch.uint8, device=G.device)
     call("bsp_spmm_t", _p(words), M, K, _p(G), _DT[G.dtype], ldg, N, _p(out), out.stride(0),
          plan.handle if plan is not None else None, _p(workspace),
          workspace.numel() * workspace.element_size(), _stream())

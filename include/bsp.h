@@ -302,6 +302,8 @@ int bsp_tune_cache_size(int* entries);
  * walked like bsp_spmm.  The backward of the forward SpMM; no reference
  * counterpart (the reference has no backward).                            */
 int bsp_spmm_t_workspace(int64_t M, int64_t K, size_t* bytes);
+/* ... and with room for the tensor-core reduction split (as for bsp_spmm). */
+int bsp_spmm_t_workspace_preferred(int64_t M, int64_t K, int64_t N, size_t* bytes);
 int bsp_spmm_t(const uint32_t* A_words, int64_t M, int64_t K, const void* G,
                int g_dtype, int64_t ldg, int64_t N, float* dX, int64_t lddx,
                const bsp_plan* plan, void* workspace, size_t workspace_bytes,
