@@ -368,22 +368,33 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
                                           : ptx::smem_desc_noswizzle_u32(a0, kLbo, kSbo);
     const uint64_t bdesc = MODE == kSddmm ? ptx::smem_desc_noswizzle_u32(b0, 16, kSdSbo) | ((uint64_t)kLayoutSw128 << 61)
                                           : ptx::smem_desc_noswizzle_u32(b0, kBox, 1024) | ((uint64_t)kLayoutSw128 << 61);
+    // The tensor pipe queues about one MMA beyond the one it runs, so every
+    // cycle this thread spends between stages is idle tensor time: the next
+    // stage's halves are read from the list while this stage issues, and the
+    // abort flag is not polled here (a warp that gives up stops arriving, and
+    // this thread's own bounded wait then ends the loop).
+    auto halves = [&](int st, int& h0, int& h1) {
+      h0 = dense_halves;
+      h1 = 0;
+      if (MODE != kSddmm && st < nstages) {
+        const int k0 = kTilesPerStage * st;
+        h0 = (lst[k0] >> 28) & 3;
+        h1 = k0 + 1 < n ? (lst[k0 + 1] >> 28) & 3 : 0;
+      }
+    };
     uint32_t started = 0;
     int i = 0;
+    int hn0, hn1;
+    halves(0, hn0, hn1);
     for (; i < nstages; i++) {
       const int s = i % kStages;
-      int hv0 = dense_halves, hv1 = 0;
-      if (MODE != kSddmm) {
-        const int k0 = kTilesPerStage * i;
-        hv0 = (lst[k0] >> 28) & 3;
-        hv1 = k0 + 1 < n ? (lst[k0 + 1] >> 28) & 3 : 0;
-      }
+      const int hv0 = hn0, hv1 = hn1;
+      halves(i + 1, hn0, hn1);
       if (!ptx::mbar_wait(&sm.full[s], (i / kStages) & 1)) {
         atomicCAS(&g_tc_error, 0, 3);
         sm.abort = 1;
         break;
       }
-      if (*(volatile int*)&sm.abort) break;
       ptx::tc_fence_after_sync();
       const uint64_t soff = (uint64_t)((s * kStageBytes) >> 4);
       const uint64_t as = adesc + soff, bs = bdesc + soff;
