@@ -368,6 +368,8 @@ def run_ours(args):
         "max_rel_diff_vs_direct": err,
         "e2e_output_matches_graph_output": e2e_matches,
     }
+    if rank == 0:
+        out["cusparse"] = _cusparse(words, K, Bs[0], launch_ms, Cd)
     if rank == 0 and ws == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
         t_full, sample = cpu_reference(cfg, cpu_sample_rows(cfg, args.cpu_seconds, threads), threads)
@@ -424,18 +426,30 @@ def run_other(args):
         return e0.elapsed_time(e1) / steps
 
     step = lambda: ops.spmm(words, K, B, plan=plan, out=C, workspace=wsp)
+    # the step replayed from a CUDA graph (no host launch cost in the time)
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream(device=dev)
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        with torch.cuda.graph(graph, stream=side):
+            step()
+    torch.cuda.synchronize()
     sampler = ClockSampler(local) if rank == 0 else None
     if sampler:
         sampler.start()
     barrier(ws)
-    ms = max_over_ranks(ws, timed(step, args.steps, max(args.warmup, 3)))
+    ms = max_over_ranks(ws, timed(graph.replay, args.steps, max(args.warmup, 3)))
     barrier(ws)
     clocks = sampler.stop() if sampler else None
     out = {"metric": METRIC, "value": ws * comp / (ms * 1e-3) / 1e9, "unit": UNIT, "n_gpus": ws,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic (seeded numpy)",
            "config": {"workload": cfg["name"], "M": M, "K": K, "N": N, "plan_ms": plan_ms,
-                      "nnz": info["nnz"], "l2": "working set %.0f MB" % (comp / 1e6)},
+                      "nnz": info["nnz"], "l2": "working set %.0f MB" % (comp / 1e6),
+                      "graph": "one step captured, replayed"},
            "effective_gflops": flops / (ms * 1e-3) / 1e9, "clocks": clocks}
     if args.config == "c3":
         occ = info["occ_tiles"]
@@ -450,7 +464,9 @@ def run_other(args):
         ms32 = timed(step32, 2, 1)
         out["fp32_form_ms"] = ms32
         out["speedup_vs_fp32_form"] = ms32 / ms
+        step()
     if rank == 0:
+        out["cusparse"] = _cusparse(words, K, B, ms, C, iters=3)
         print(json.dumps(out), flush=True)
     plan.close()
 
@@ -609,6 +625,10 @@ def run_fwd_bwd(args):
                       "frac": dense / (ms * 1e-3) / 1e12 / tp, "peak_source": tkind},
            "gbs_compulsory": comp / (ms * 1e-3) / 1e9, "clocks": clocks}
     if rank == 0:
+        # cuSPARSE on the forward product Y = A·X (its SpMM has no fused
+        # transposed-bitmap or SDDMM counterpart here)
+        ms_fwd = _timed(lambda: ops.spmm(words, K, X, plan=plan, out=Y, workspace=wsp), 5, 2)
+        out["cusparse_forward"] = dict(_cusparse(words, K, X, ms_fwd, Y, iters=3), ours_forward_ms=ms_fwd)
         print(json.dumps(out), flush=True)
     plan.close()
 
@@ -626,6 +646,30 @@ def _timed(fn, steps, warm):
     e1.record(cur)
     torch.cuda.synchronize()
     return e0.elapsed_time(e1) / steps
+
+
+def _cusparse(words, K, B, ours_ms, ours_C, iters=5):
+    """cuSPARSE's CSR SpMM on the same A (values 1) and B: the reference's
+    library baseline (source/src/main.cu:1061-1131), outside every timed
+    region of this benchmark.  `ms` is the warm mean over `iters` calls,
+    `first_call_ms` the reference's own measure (workspace query + allocation
+    + one call).  Any failure becomes an `unavailable` entry."""
+    import torch
+    from bitwise_spgemm_gb300 import cusparse_baseline as CS
+    ok, why = CS.available()
+    if not ok:
+        return {"unavailable": why}
+    try:
+        off, cols = CS.csr_from_words(words, K)
+        C, ms, first = CS.spmm_csr(off, cols, B, words.shape[0], warmup=2, iters=iters)
+        torch.cuda.synchronize()
+        diff = (C - ours_C).abs().max().item() / max(ours_C.abs().max().item(), 1e-30)
+        del off, cols, C
+        return {"ms": ms, "first_call_ms": first, "alg": "CUSPARSE_SPMM_ALG_DEFAULT, CSR int32, values 1",
+                "dtype": "f32" if B.dtype == torch.float32 else "bf16 in, f32 out",
+                "speedup_ours_vs_cusparse": ms / ours_ms, "max_rel_diff_vs_ours": diff}
+    except (RuntimeError, ValueError) as exc:
+        return {"unavailable": str(exc)}
 
 
 def _cpu_rows(fn, M, rows0=64, budget=5.0):

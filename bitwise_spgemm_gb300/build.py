@@ -3,7 +3,8 @@
 Every ``csrc/*.cu`` is compiled by nvcc in parallel into ``_build/`` and
 linked into ``bitwise_spgemm_gb300/libbsp.so`` (CUDA runtime linked
 statically), then the C++ harness ``harness/bsp_harness`` is linked against
-it.  No cmake, one ``-gencode``; rebuilds only changed sources.
+it, and cuSPARSE's CSR SpMM (the reference's library baseline, timing only)
+is built into its own ``libbsp_cusparse.so``.  No cmake, one ``-gencode``; rebuilds only changed sources.
 """
 import concurrent.futures as cf
 import glob
@@ -64,6 +65,30 @@ def build_harness(force=False):
     return HARNESS
 
 
+CUSPARSE_SRC = os.path.join(PKG, "baselines", "cusparse_spmm.cpp")
+CUSPARSE_LIB = os.path.join(PKG, "libbsp_cusparse.so")
+
+
+def build_cusparse_baseline(force=False):
+    """cuSPARSE's CSR SpMM, the reference's library baseline (timing and
+    cross-checks only), as its own libbsp_cusparse.so next to libbsp.so.
+    Returns None, with the reason printed, when the toolkit cannot link it:
+    the bitmap library does not depend on it."""
+    newest = max(os.path.getmtime(p) for p in [CUSPARSE_SRC] + glob.glob(os.path.join(INCLUDE, "*.h")))
+    if not force and os.path.exists(CUSPARSE_LIB) and os.path.getmtime(CUSPARSE_LIB) >= newest:
+        return CUSPARSE_LIB
+    libdir = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc()))), "lib64")
+    tmp = CUSPARSE_LIB + ".tmp%d" % os.getpid()
+    try:
+        subprocess.check_call([nvcc(), "-O2", "-std=c++17", "-shared", "-Xcompiler", "-fPIC", "-I", INCLUDE,
+                               CUSPARSE_SRC, "-o", tmp, "-lcusparse", "-Xlinker", "-rpath," + libdir])
+    except (subprocess.CalledProcessError, OSError) as exc:
+        print("cuSPARSE baseline not built: %s" % exc)
+        return None
+    os.replace(tmp, CUSPARSE_LIB)
+    return CUSPARSE_LIB
+
+
 def build(force=False, jobs=None):
     os.makedirs(OBJ, exist_ok=True)
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
@@ -76,6 +101,7 @@ def build(force=False, jobs=None):
         subprocess.check_call([nvcc()] + ARCH + ["-shared", "-o", tmp] + objs)
         os.replace(tmp, LIB)
     build_harness(force)
+    build_cusparse_baseline(force)
     return LIB
 
 
