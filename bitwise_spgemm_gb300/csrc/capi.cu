@@ -314,8 +314,8 @@ int bsp_spmm_workspace(const bsp_plan* plan, int64_t N, size_t* bytes) {
 int bsp_spmm_workspace_preferred(const bsp_plan* plan, int64_t N, size_t* bytes) {
   BSP_TRY(bsp_spmm_workspace(plan, N, bytes));
   if (plan) {
-    const size_t split = tc_split_bytes(plan->M, N, ceil_div(plan->K, 32));
-    if (split > *bytes) *bytes = split;
+    const size_t tc = tc_preferred_bytes(plan->M, N, plan->K);
+    if (tc > *bytes) *bytes = tc;
   }
   return BSP_OK;
 }
@@ -600,8 +600,8 @@ int bsp_csr_to_tiled(const int32_t* row_ptr, const int32_t* col_idx, const void*
 int bsp_spmm_t_workspace_preferred(int64_t M, int64_t K, int64_t N, size_t* bytes) {
   if (!bytes || M < 0 || K < 0 || N < 0) return BSP_ERR_INVALID_ARG;
   BSP_TRY(bsp_spmm_t_workspace(M, K, bytes));
-  const size_t split = tc_split_bytes(K, N, ceil_div(M, 32));
-  if (split > *bytes) *bytes = split;
+  const size_t tc = tc_preferred_bytes(K, N, M);
+  if (tc > *bytes) *bytes = tc;
   return BSP_OK;
 }
 

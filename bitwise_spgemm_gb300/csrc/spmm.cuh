@@ -68,12 +68,18 @@ int64_t tc_max_reduction();
 int tc_occupancy_t_words(int64_t M);
 int launch_occupancy(const uint32_t* A, int64_t M, int64_t K, uint32_t* occ, uint32_t* occT,
                      unsigned long long* count, unsigned long long* countT, cudaStream_t s);
-// ws (optional): room for split-K partials; used when the output grid is
-// small and ws_bytes ≥ tc_split_bytes(...), else ignored.
+// ws (optional): room for split-K partials (used when the output grid is
+// small and ws_bytes ≥ tc_split_bytes(...)) and, after them, for B in tile
+// order (used when the rest holds tc_tiled_b_bytes(...)); else ignored.
 int launch_spmm_tc(const SpmmArgs& a, const uint32_t* occ, cudaStream_t s, void* ws = nullptr,
                    size_t ws_bytes = 0);
 int tc_split_count(int64_t out_rows, int64_t out_cols, int64_t red_tiles);
 size_t tc_split_bytes(int64_t out_rows, int64_t out_cols, int64_t red_tiles);
+// B (fwd) / G (trans) copied into tile order for one bulk copy per tile: the
+// workspace it takes, and the workspace with which the tensor-core launch
+// both splits the reduction (when it would) and tiles B.
+size_t tc_tiled_b_bytes(int64_t red_rows, int64_t cols);
+size_t tc_preferred_bytes(int64_t out_rows, int64_t out_cols, int64_t red_rows);
 // dX[K][N] = Aᵀ·G on the tensor cores, Aᵀ read from A's row words
 int launch_spmm_t_tc(const uint32_t* A, int64_t M, int64_t K, const void* G, int gdt, int64_t ldg, int64_t N,
                      float* dX, int64_t lddx, const uint32_t* occT, cudaStream_t s, void* ws = nullptr, size_t ws_bytes = 0);

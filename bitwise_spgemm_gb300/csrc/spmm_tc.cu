@@ -114,6 +114,11 @@ struct TcArgs {
   // (row stride ldp); a reduction kernel adds the slices into C
   float* part;
   int64_t ldp, part_stride;
+  // fwd / trans: B (or G) already in shared-memory order (k_tile_b), one
+  // 16 KB block per (32-row tile, 256-column block), bt_cb blocks per tile
+  // row; nullptr = B by TMA tensor boxes
+  const uint8_t* bt;
+  int64_t bt_cb;
   // batched form (kBatch): CTA b runs work item b of the batch
   const BatchProblemTc* bprobs;
   const int4* items;  // {problem, 256-row block, 256-column block, K tiles}
@@ -285,13 +290,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
         const int s = i % kStages;
         const uint32_t w0 = wq[0];
         const uint32_t wnew = load_word(kTilesPerStage * (i + kWordAhead) + u);
+        // (no abort poll on this path: a role that gives up stops arriving,
+        // and every other role's own bounded wait then ends its loop)
         int go = 1;
-        if (lane == 0) {
-          if (i >= kStages && !ptx::mbar_wait(&sm.empty[s], ((i / kStages) - 1) & 1)) {
-            atomicCAS(&g_tc_error, 0, 3);
-            sm.abort = 1;
-          }
-          go = !*(volatile int*)&sm.abort;
+        if (lane == 0 && i >= kStages && !ptx::mbar_wait(&sm.empty[s], ((i / kStages) - 1) & 1)) {
+          atomicCAS(&g_tc_error, 0, 3);
+          sm.abort = 1;
+          go = 0;
         }
         if (!__shfl_sync(kFull, go, 0)) break;
         if (kTilesPerStage * i + u < n) {
@@ -331,7 +336,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
         sm.abort = 1;
         break;
       }
-      if (*(volatile int*)&sm.abort) break;
       const uint32_t fb = f0 + s * 8, as = a0 + s * kStageBytes, bs = b0 + s * kStageBytes;
       if (MODE == kSddmm) {
         // G rows row0.. and X rows col0.. (256 each), N columns i*64..
@@ -344,6 +348,15 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
         const bool two = k0 + 1 < n;
         const int t0 = lst[k0] & 0x0fffffff;
         ptx::mbar_arrive_expect_tx(&sm.full[s], (two ? 2 : 1) * nbox * kBox);
+        if (MODE != kBatch && a.bt) {
+          // tiled B: the tile's first nbox atoms are one contiguous copy
+          const uint8_t* src = a.bt + ((int64_t)t0 * a.bt_cb + blockIdx.y) * kBTile;
+          ptx::bulk_g2s(sm.b[s], src, nbox * kBox, &sm.full[s]);
+          if (two)
+            ptx::bulk_g2s(sm.b[s] + kBTile, a.bt + ((int64_t)(lst[k0 + 1] & 0x0fffffff) * a.bt_cb + blockIdx.y) * kBTile,
+                          nbox * kBox, &sm.full[s]);
+          continue;
+        }
 #pragma unroll
         for (int j = 0; j < kTcN / kBoxCols; j++)
           if (j < nbox) ptx::tma_load_2d_u32(bs + j * kBox, bmap, (int)col0 + j * kBoxCols, t0 * kTcK, fb);
@@ -371,8 +384,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
     // The tensor pipe queues about one MMA beyond the one it runs, so every
     // cycle this thread spends between stages is idle tensor time: the next
     // stage's halves are read from the list while this stage issues, and the
-    // abort flag is not polled here (a warp that gives up stops arriving, and
-    // this thread's own bounded wait then ends the loop).
+    // abort flag is not polled here either.
     auto halves = [&](int st, int& h0, int& h1) {
       h0 = dense_halves;
       h1 = 0;
@@ -490,6 +502,30 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
   if (warp == kMmaWarp) {
     ptx::tc_fence_after_sync();
     ptx::tmem_dealloc(tmem, kTmemCols);
+  }
+}
+
+// B (fwd) or G (trans) [R][N] of 16-bit values -> the shared-memory order
+// of the tensor-core kernel's B stage, so that a tile arrives by one
+// contiguous bulk copy instead of four tensor boxes of 32 rows: block (t, cb)
+// (16 KB, t = 32-row tile, cb = 256-column block) holds four 64-column atoms
+// of 4 KB; in atom j, row r occupies 128 bytes whose 16-byte chunk c sits at
+// position c ^ (r % 8) (the 128-byte swizzle, as a TMA load into a
+// 1024-byte aligned stage writes it).  Rows past R and columns past N are
+// zero.  One thread per 16-byte chunk: a warp reads 512 contiguous bytes of
+// one row and writes four 128-byte runs.
+__global__ void __launch_bounds__(256) k_tile_b(const uint8_t* __restrict__ B, int64_t R, int64_t N, int64_t ldb,
+                                                int64_t ntiles, int64_t ncb, uint4* __restrict__ bt) {
+  const int64_t total = ntiles * ncb * (kBTile / 16);
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t blk = e >> 10;
+    const int in = (int)(e & 1023);
+    const int r = in >> 5, j = (in >> 3) & 3, c = in & 7;
+    const int64_t t = blk / ncb, cb = blk - t * ncb;
+    const int64_t row = t * kTcK + r, col = cb * kTcN + j * kBoxCols + c * 8;
+    uint4 v = make_uint4(0u, 0u, 0u, 0u);
+    if (row < R && col < N) v = __ldg(reinterpret_cast<const uint4*>(B + (row * ldb + col) * 2));
+    bt[blk * 1024 + j * 256 + r * 8 + (c ^ (r & 7))] = v;
   }
 }
 
@@ -647,7 +683,33 @@ size_t tc_split_bytes(int64_t out_rows, int64_t out_cols, int64_t red_tiles) {
   return S > 1 ? (size_t)S * (size_t)out_rows * (size_t)(ceil_div(out_cols, 4) * 4) * sizeof(float) + 256 : 0;
 }
 
+// B (or G) in tile order: every (32-row tile, 256-column block) is 16 KB.
+size_t tc_tiled_b_bytes(int64_t red_rows, int64_t cols) {
+  return (size_t)ceil_div(red_rows, kTcK) * (size_t)ceil_div(cols, kTcN) * kBTile + 1024;
+}
+
+// Tiling B costs a read and a write of it; it pays where many row blocks
+// read every B tile (measured on GB300: 16384 rows, 64 blocks, 0.84 -> 0.80
+// ms; 4096 rows, 16 blocks, forward + backward 0.76 -> 0.79 ms).
+constexpr int64_t kTiledMinRowBlocks = 32;
+
+bool tc_tiles_b(int64_t out_rows) { return ceil_div(out_rows, kCtaM) >= kTiledMinRowBlocks; }
+
+size_t tc_preferred_bytes(int64_t out_rows, int64_t out_cols, int64_t red_rows) {
+  return tc_split_bytes(out_rows, out_cols, ceil_div(red_rows, kTcK)) +
+         (tc_tiles_b(out_rows) ? tc_tiled_b_bytes(red_rows, out_cols) : 0);
+}
+
 namespace {
+
+// BSP_TC_TILED_B=0 keeps B on tensor boxes even with room for the tiled copy.
+bool tiled_b_enabled() {
+  static const bool on = [] {
+    const char* e = getenv("BSP_TC_TILED_B");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
 
 template <int MODE>
 int launch_tc(TcArgs a, cudaStream_t s, void* ws = nullptr, size_t ws_bytes = 0) {
@@ -655,6 +717,7 @@ int launch_tc(TcArgs a, cudaStream_t s, void* ws = nullptr, size_t ws_bytes = 0)
   const int64_t cols = MODE == kSddmm ? a.K : a.N;
   if (rows == 0 || cols == 0) return BSP_OK;
   int splits = 1;
+  size_t used = 0;
   if (MODE != kSddmm && ws) {
     const int64_t red_tiles = ceil_div(MODE == kFwd ? a.K : a.M, kTcK);
     const int S = tc_split_count(rows, cols, red_tiles);
@@ -663,8 +726,13 @@ int launch_tc(TcArgs a, cudaStream_t s, void* ws = nullptr, size_t ws_bytes = 0)
       a.part = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(ws) + 255) & ~(uintptr_t)255);
       a.ldp = ceil_div(cols, 4) * 4;
       a.part_stride = rows * a.ldp;
+      used = tc_split_bytes(rows, cols, red_tiles);
     }
   }
+  // B in tile order when the rest of the workspace holds it (else tensor boxes)
+  const int64_t red_rows = MODE == kFwd ? a.K : a.M;
+  const bool tiled = MODE != kSddmm && ws && tc_tiles_b(rows) && ws_bytes >= used + tc_tiled_b_bytes(red_rows, cols) &&
+                     tiled_b_enabled();
   const dim3 grid((unsigned)ceil_div(rows, kCtaM), (unsigned)ceil_div(cols, kTcN), (unsigned)splits);
   if (ceil_div(cols, kTcN) > 65535 || ceil_div(rows, kCtaM) > 0x7fffffff) return BSP_ERR_CAPACITY;
   if (a.N > INT32_MAX || a.M > INT32_MAX || a.K > INT32_MAX) return BSP_ERR_CAPACITY;
@@ -679,6 +747,18 @@ int launch_tc(TcArgs a, cudaStream_t s, void* ws = nullptr, size_t ws_bytes = 0)
     // B [K][N] (fwd) or G [M][N] (trans), 64 columns x 32 reduction rows per box
     BSP_TRY(make_map(&mb, a.B, a.bdt, MODE == kFwd ? a.K : a.M, a.N, a.ldb, kBoxCols, kTcK,
                      CU_TENSOR_MAP_SWIZZLE_128B));
+  }
+  if (tiled) {
+    const int64_t ntiles = ceil_div(red_rows, kTcK), ncb = ceil_div(cols, kTcN);
+    uint8_t* bt = reinterpret_cast<uint8_t*>(
+        (reinterpret_cast<uintptr_t>(static_cast<char*>(ws) + used) + 1023) & ~(uintptr_t)1023);
+    const int64_t work = ntiles * ncb * (kBTile / 16);
+    const int64_t cap = (int64_t)num_sms() * 16;
+    k_tile_b<<<(unsigned)(ceil_div(work, 256) < cap ? ceil_div(work, 256) : cap), 256, 0, s>>>(
+        static_cast<const uint8_t*>(a.B), red_rows, cols, a.ldb, ntiles, ncb, reinterpret_cast<uint4*>(bt));
+    BSP_LAUNCHED();
+    a.bt = bt;
+    a.bt_cb = ncb;
   }
   if (a.bdt == BSP_BF16) BSP_TRY((launch_mode<__nv_bfloat16, MODE>(a, ma, mb, grid, s)));
   else if (a.bdt == BSP_F16) BSP_TRY((launch_mode<__half, MODE>(a, ma, mb, grid, s)));

@@ -200,12 +200,14 @@ int bsp_plan_get_info(const bsp_plan* plan, bsp_plan_info* info);
 /* Device workspace (bytes) that bsp_spmm needs for this plan and N. */
 int bsp_spmm_workspace(const bsp_plan* plan, int64_t N, size_t* bytes);
 
-/* Workspace (bytes, ≥ the above) with which the tensor-core path may also
- * split the reduction: when the output has fewer 256x256 tiles than half
- * the SMs, up to 8 slices of the occupied K tiles run on separate CTAs and
- * their FP32 partials (kept in the workspace) are added in a fixed order.
- * A smaller workspace only turns the split off.  bsp_spmm_t uses its own
- * workspace the same way when it is large enough.                        */
+/* Workspace (bytes, ≥ the above) with which the tensor-core path (16-bit
+ * B) also (1) splits the reduction: when the output has fewer 256x256 tiles
+ * than half the SMs, up to 8 slices of the occupied K tiles run on separate
+ * CTAs and their FP32 partials (kept in the workspace) are added in a fixed
+ * order; and (2) copies B into tile order first (ceil(K/32)·ceil(N/256)
+ * blocks of 16 KB), so that each tile reaches shared memory as one bulk
+ * copy.  A smaller workspace only turns these off (results are identical).
+ * bsp_spmm_t uses its own workspace the same way when it is large enough. */
 int bsp_spmm_workspace_preferred(const bsp_plan* plan, int64_t N, size_t* bytes);
 
 /* C[M×N] (FP32, row stride ldc) = A·B, A given by its packed words and,

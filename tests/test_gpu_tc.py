@@ -129,3 +129,49 @@ def test_tc_split_k(force_tc, M, K, N, p):
     assert np.array_equal(Ca, Cb)
     mx, _, _ = O.rel_errors(Ca, O.spmm_f64(words, K, Bexact), O.spmm_abs_f64(words, K, Bexact))
     assert mx <= TOL, mx
+
+
+@pytest.mark.parametrize("M,K,N", [(300, 200, 264), (1000, 1000, 512), (513, 4096, 776), (64, 40, 8),
+                                   (8200, 300, 72), (600, 8300, 40)])
+def test_tiled_b_matches_tensor_boxes(force_tc, M, K, N):
+    # the preferred workspace copies B (and G) into tile order, one bulk copy
+    # per tile, where the output has many row blocks; the minimum keeps TMA
+    # tensor boxes.  The shared-memory bytes are the same, so integer-valued
+    # operands (exact in any order) give identical results, including ragged
+    # edges (K and M tails, a last column block of 8 or 8 < n < 64 columns);
+    # N(0,1) operands stay within the precision-form tolerance either way.
+    rng = np.random.default_rng(M + 3 * K + N)
+    bits = rng.random((M, K)) < 0.2
+    words = W.pack_bits(bits)
+    wd = words_dev(words)
+    plan = ops.Plan(wd, K)
+    ws_pref = torch.empty(plan.workspace_bytes(N), dtype=torch.uint8, device="cuda")
+    ws_min = torch.empty(max(plan.workspace_bytes(N, preferred=False), 1), dtype=torch.uint8, device="cuda")
+    Bi, Bie = _b16(rng.integers(-8, 9, (K, N)).astype(np.float32), "bf16")
+    ref = O.spmm_f64(words, K, Bie)
+    for ws in (ws_pref, ws_min):
+        assert np.array_equal(ops.spmm(wd, K, Bi, plan=plan, workspace=ws).cpu().numpy().astype(np.float64), ref)
+    B, Bexact = _b16(rng.standard_normal((K, N)).astype(np.float32), "bf16")
+    for ws in (ws_pref, ws_min):
+        C = ops.spmm(wd, K, B, plan=plan, workspace=ws).cpu().numpy()
+        mx, _, _ = O.rel_errors(C, O.spmm_f64(words, K, Bexact), O.spmm_abs_f64(words, K, Bexact))
+        assert mx <= TOL
+    assert capi.device_status() == 0
+    # transposed product: G [M][N] tiled over M
+    n_min, n_pref = _t_workspaces(M, K, N)
+    Gi, Gie = _b16(rng.integers(-8, 9, (M, N)).astype(np.float32), "bf16")
+    ref_t = O.spmm_t_f64(words, M, K, Gie)
+    for nb in (n_pref, n_min):
+        ws = torch.empty(nb, dtype=torch.uint8, device="cuda")
+        dX = ops.spmm_t(wd, M, K, Gi, plan=plan, workspace=ws).cpu().numpy()
+        assert np.array_equal(dX.astype(np.float64), ref_t)
+    assert capi.device_status() == 0
+
+
+def _t_workspaces(M, K, N):
+    import ctypes
+    a, b = ctypes.c_size_t(), ctypes.c_size_t()
+    capi.call("bsp_spmm_t_workspace", M, K, ctypes.byref(a))
+    capi.call("bsp_spmm_t_workspace_preferred", M, K, N, ctypes.byref(b))
+    assert b.value >= a.value
+    return a.value, b.value
