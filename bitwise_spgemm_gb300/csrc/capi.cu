@@ -268,7 +268,7 @@ static int run_spmm(SpmmArgs a, const bsp_plan* plan, bool vec, const TuneSched&
                     size_t workspace_bytes, cudaStream_t s) {
   // Tensor cores for 16-bit B when the occupied bit tiles make a dense
   // contraction cheaper than gathering B rows.
-  if (sc.engine == 1) return launch_spmm_tc(a, plan->occ, s, workspace, workspace_bytes);
+  if (sc.engine == 1) return launch_spmm_tc(a, plan->occ, plan->wordsT, s, workspace, workspace_bytes);
   const int64_t N = a.N, K = a.K;
   const bool proto = plan && plan->mode == BSP_PLAN_PROTO && vec;
   if (proto) {
@@ -639,7 +639,7 @@ int bsp_spmm_t(const uint32_t* A_words, int64_t M, int64_t K, const void* G, int
     const double tc = (double)plan->occT_tiles * 128.0 * 32.0 * (double)N * 2.0 / 1.2e15;
     const double cc = (double)plan->nnz * (double)N * (double)esz / 8e12;
     if (e ? e[0] == '1' : tc < cc)
-      return launch_spmm_t_tc(A_words, M, K, G, g_dtype, ldg, N, dX, lddx, plan->occT, s, workspace,
+      return launch_spmm_t_tc(A_words, M, K, G, g_dtype, ldg, N, dX, lddx, plan->occT, plan->wordsT, s, workspace,
                               workspace_bytes);
   }
   // CUDA cores: transpose the bits into the workspace, then walk the rows of Aᵀ

@@ -477,6 +477,10 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
   const size_t p_dl = ptake(sizeof(int32_t) * M);
   const size_t p_occ = ptake(sizeof(uint32_t) * ceil_div(M, 128) * tc_occupancy_words(K));
   const size_t p_occT = ptake(sizeof(uint32_t) * ceil_div(K, 128) * tc_occupancy_t_words(M));
+  // A's words by column: the tensor-core producers then load the words of
+  // 32 consecutive rows (forward) or columns (transposed) as one 128-byte run
+  const bool with_wt = (double)M * (double)Kw * 4.0 <= (double)(1ull << 32) && ceil_div(M, 32) <= 65535;
+  const size_t p_wt = ptake(with_wt ? sizeof(uint32_t) * (size_t)Kw * (size_t)M : 0);
   void* parena = nullptr;
   BSP_CUDA(plan_alloc(&parena, poff ? poff : 16, s));
   plan->arena = parena;
@@ -488,6 +492,10 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
   plan->occ = (uint32_t*)(Pa + p_occ);
   plan->occT = (uint32_t*)(Pa + p_occT);
   BSP_TRY(launch_occupancy(words, M, K, plan->occ, plan->occT, stats + 5, stats + 6, s));
+  if (with_wt) {
+    plan->wordsT = (uint32_t*)(Pa + p_wt);
+    BSP_TRY(launch_transpose_words(words, M, Kw, plan->wordsT, s));
+  }
   plan->n_proto = ncl;
 
   if (ncl > 0) {

@@ -18,6 +18,7 @@ struct bsp_plan {
   uint32_t* occ = nullptr;         // occupied 32-column K tiles per 128-row block (tensor-core path)
   int64_t occ_tiles = 0;           // number of occupied (128-row, 32-column) tiles
   uint32_t* occT = nullptr;        // occupied 32-row tiles per 128-column block (transposed product)
+  uint32_t* wordsT = nullptr;      // A's words column by column, [Kw][M] (tensor-core word loads), or null
   int64_t occT_tiles = 0;
 };
 

@@ -71,8 +71,11 @@ int launch_occupancy(const uint32_t* A, int64_t M, int64_t K, uint32_t* occ, uin
 // ws (optional): room for split-K partials (used when the output grid is
 // small and ws_bytes ≥ tc_split_bytes(...)) and, after them, for B in tile
 // order (used when the rest holds tc_tiled_b_bytes(...)); else ignored.
-int launch_spmm_tc(const SpmmArgs& a, const uint32_t* occ, cudaStream_t s, void* ws = nullptr,
+// At (optional): A's words column by column ([Kw][M], launch_transpose_words)
+// for coalesced word loads; null = loads from the rows.
+int launch_spmm_tc(const SpmmArgs& a, const uint32_t* occ, const uint32_t* At, cudaStream_t s, void* ws = nullptr,
                    size_t ws_bytes = 0);
+int launch_transpose_words(const uint32_t* words, int64_t M, int64_t Kw, uint32_t* At, cudaStream_t s);
 int tc_split_count(int64_t out_rows, int64_t out_cols, int64_t red_tiles);
 size_t tc_split_bytes(int64_t out_rows, int64_t out_cols, int64_t red_tiles);
 // B (fwd) / G (trans) copied into tile order for one bulk copy per tile: the
@@ -82,7 +85,7 @@ size_t tc_tiled_b_bytes(int64_t red_rows, int64_t cols);
 size_t tc_preferred_bytes(int64_t out_rows, int64_t out_cols, int64_t red_rows);
 // dX[K][N] = Aᵀ·G on the tensor cores, Aᵀ read from A's row words
 int launch_spmm_t_tc(const uint32_t* A, int64_t M, int64_t K, const void* G, int gdt, int64_t ldg, int64_t N,
-                     float* dX, int64_t lddx, const uint32_t* occT, cudaStream_t s, void* ws = nullptr, size_t ws_bytes = 0);
+                     float* dX, int64_t lddx, const uint32_t* occT, const uint32_t* At, cudaStream_t s, void* ws = nullptr, size_t ws_bytes = 0);
 // dA[M][K] = (G·Xᵀ) at A's set bits, 0 elsewhere, on the tensor cores
 int launch_sddmm_tc(const uint32_t* A, int64_t M, int64_t K, const void* G, int64_t ldg, const void* X,
                     int64_t ldx, int dt, int64_t N, float* dA, int64_t ldda, cudaStream_t s);

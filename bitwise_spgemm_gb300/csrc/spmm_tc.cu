@@ -121,6 +121,8 @@ struct TcArgs {
   int64_t bt_cb;
   // batched form (kBatch): CTA b runs work item b of the batch
   const BatchProblemTc* bprobs;
+  // fwd / trans: A's words column by column ([Kw][M]) for coalesced loads, or null
+  const uint32_t* At;
   const int4* items;  // {problem, 256-row block, 256-column block, K tiles}
 };
 
@@ -277,11 +279,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
         const int t = lst[k] & 0x0fffffff;
         if (kFwdLike) {
           const int64_t arow = row0 + r;
-          return arow < gM ? __ldg(gA + arow * gKw + t) : 0u;
+          if (arow >= gM) return 0u;
+          return (MODE != kBatch && a.At) ? __ldg(a.At + (int64_t)t * gM + arow) : __ldg(gA + arow * gKw + t);
         }
         const int64_t arow = (int64_t)t * kTcK + (r & 31);
         const int64_t wcol = row0 / 32 + (r >> 5);
-        return (arow < gM && wcol < gKw) ? __ldg(gA + arow * gKw + wcol) : 0u;
+        if (arow >= gM || wcol >= gKw) return 0u;
+        return a.At ? __ldg(a.At + wcol * gM + arow) : __ldg(gA + arow * gKw + wcol);
       };
       uint32_t wq[kWordAhead];
 #pragma unroll
@@ -577,6 +581,32 @@ int tc_occupancy_words(int64_t K) { return (int)ceil_div(ceil_div(K, 32), 32); }
 int64_t tc_max_reduction() { return (int64_t)kListMax * kTcK; }
 int tc_occupancy_t_words(int64_t M) { return (int)ceil_div(ceil_div(M, 32), 32); }
 
+// words [M][Kw] -> At [Kw][M] through 32x32 shared-memory tiles (coalesced
+// on both sides).
+__global__ void __launch_bounds__(256) k_transpose_words(const uint32_t* __restrict__ w, int64_t M, int64_t Kw,
+                                                         uint32_t* __restrict__ At) {
+  __shared__ uint32_t tile[32][33];
+  const int64_t c0 = (int64_t)blockIdx.x * 32, r0 = (int64_t)blockIdx.y * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int k = ty; k < 32; k += 8) {
+    const int64_t r = r0 + k, c = c0 + tx;
+    tile[k][tx] = (r < M && c < Kw) ? __ldg(w + r * Kw + c) : 0u;
+  }
+  __syncthreads();
+  for (int k = ty; k < 32; k += 8) {
+    const int64_t c = c0 + k, r = r0 + tx;
+    if (c < Kw && r < M) At[c * M + r] = tile[tx][k];
+  }
+}
+
+int launch_transpose_words(const uint32_t* words, int64_t M, int64_t Kw, uint32_t* At, cudaStream_t s) {
+  if (M == 0 || Kw == 0) return BSP_OK;
+  if (ceil_div(M, 32) > 65535) return BSP_ERR_CAPACITY;
+  k_transpose_words<<<dim3((unsigned)ceil_div(Kw, 32), (unsigned)ceil_div(M, 32)), 256, 0, s>>>(words, M, Kw, At);
+  BSP_LAUNCHED();
+  return BSP_OK;
+}
+
 int launch_occupancy(const uint32_t* A, int64_t M, int64_t K, uint32_t* occ, uint32_t* occT,
                      unsigned long long* count, unsigned long long* countT, cudaStream_t s) {
   const int64_t Kw = ceil_div(K, 32);
@@ -774,8 +804,10 @@ int launch_tc(TcArgs a, cudaStream_t s, void* ws = nullptr, size_t ws_bytes = 0)
 }
 }  // namespace
 
-int launch_spmm_tc(const SpmmArgs& sa, const uint32_t* occ, cudaStream_t s, void* ws, size_t ws_bytes) {
+int launch_spmm_tc(const SpmmArgs& sa, const uint32_t* occ, const uint32_t* At, cudaStream_t s, void* ws,
+                   size_t ws_bytes) {
   TcArgs a = {};
+  a.At = At;
   a.A = sa.A;
   a.M = sa.M;
   a.K = sa.K;
@@ -792,8 +824,10 @@ int launch_spmm_tc(const SpmmArgs& sa, const uint32_t* occ, cudaStream_t s, void
 }
 
 int launch_spmm_t_tc(const uint32_t* A, int64_t M, int64_t K, const void* G, int gdt, int64_t ldg, int64_t N,
-                     float* dX, int64_t lddx, const uint32_t* occT, cudaStream_t s, void* ws, size_t ws_bytes) {
+                     float* dX, int64_t lddx, const uint32_t* occT, const uint32_t* At, cudaStream_t s, void* ws,
+                     size_t ws_bytes) {
   TcArgs a = {};
+  a.At = At;
   a.A = A;
   a.M = M;
   a.K = K;
