@@ -67,6 +67,10 @@ constexpr int kWordAhead = 4;                 // A words are loaded this many st
 // bits 0-27, which 128-row halves have bits in bits 28-29.
 constexpr int kListMax = 4096;
 constexpr uint32_t kTmemCols = 512;       // two 128x256 FP32 accumulators
+// Epilogue staging: a warp's 32 rows x 32 columns of FP32 in the idle stage
+// memory, rows 36 floats apart (16-byte aligned; the row-wise float4 writes
+// and the column-block float4 reads are both free of bank conflicts).
+constexpr int kEpiStride = 36;
 using tc::kLbo;
 using tc::kSbo;
 using tc::kLayoutSw128;
@@ -449,22 +453,32 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
   // ---------------- epilogue (producer warps) ----------------
   // Warp w reads TMEM lanes 32*(w%4).. (a warp may only touch its own
   // quarter of the lanes) of accumulator (w/4)%2, columns 128*(w/8)..; a
-  // thread stores 128 columns of one output row.
+  // thread holds 32 columns of one output row at a time.  Products other
+  // than the SDDMM pass them through a 32x32 tile of the (now idle) stage
+  // memory, so that each store instruction writes four whole 128-byte rows
+  // of C instead of 16 bytes in each of 32 rows.
   if (warp < kProducerWarps) {
     const int h = (warp >> 2) & 1, q = warp & 3, cg = warp >> 3;
     const bool have = (sm.seen >> h) & 1;
-    bool ok = ptx::mbar_wait(&sm.done, 0);
-    if (!ok) {
+    // warp-uniform flags: the TMEM loads and the tile hand-off below are
+    // collective over the warp
+    const bool ok = __all_sync(kFull, ptx::mbar_wait(&sm.done, 0));
+    if (!ok && lane == 0) {
       atomicCAS(&g_tc_error, 0, 3);
       sm.abort = 1;
     }
     ptx::tc_fence_after_sync();
-    const int64_t row = row0 + h * kTcM + q * 32 + lane;
-    float* crow = (gridDim.z > 1 ? a.part + (int64_t)blockIdx.z * a.part_stride + row * a.ldp
-                                 : gC + row * gldc) + col0 + cg * (kTcN / 2);
-    const bool live = row < out_rows && ok && !*(volatile int*)&sm.abort;
+    const bool wlive = __all_sync(kFull, ok && !*(volatile int*)&sm.abort);
+    const int64_t rbase = row0 + h * kTcM + q * 32;  // the warp's first row
+    const int64_t row = rbase + lane;
+    const bool split = gridDim.z > 1;
+    float* cbase = split ? a.part + (int64_t)blockIdx.z * a.part_stride : gC;
+    const int64_t cld = split ? a.ldp : gldc;
+    const int64_t ccol = col0 + cg * (kTcN / 2);  // the warp's first column
+    const bool live = row < out_rows && wlive;
     const uint32_t* arow = gA + row * gKw;
     const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * kTcN + cg * (kTcN / 2));
+    float* tile = reinterpret_cast<float*>(sm.a[0]) + warp * 32 * kEpiStride;
     // columns of this warp's half that hold output: up to 64·nbox of the tile
     const int c8_end = (int)max(0, min(kTcN / 2, nbox * kBoxCols - cg * (kTcN / 2))) / 8;
     for (int c8 = 0; c8 < c8_end; c8 += 4) {
@@ -479,26 +493,49 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
 #pragma unroll
           for (int v = 0; v < 8; v++) r[u][v] = 0u;
       }
-      if (!live) continue;
+      if (MODE == kSddmm) {
+        if (!live) continue;
+        float* crow = cbase + row * cld + ccol;
 #pragma unroll
-      for (int u = 0; u < 4; u++) {
-        const int col = (c8 + u) * 8;
-        const int64_t gcol = col0 + cg * (kTcN / 2) + col;
-        if (gcol >= out_cols) continue;
-        if (MODE == kSddmm) {  // keep the set bits of A's row only
+        for (int u = 0; u < 4; u++) {
+          const int col = (c8 + u) * 8;
+          const int64_t gcol = ccol + col;
+          if (gcol >= out_cols) continue;
+          // keep the set bits of A's row only
           const uint32_t bits = (__ldg(arow + gcol / 32) >> (gcol & 31)) & 0xffu;
 #pragma unroll
           for (int v = 0; v < 8; v++)
             if (!((bits >> v) & 1u)) r[u][v] = 0u;
-        } else {  // the bit operand held 2.0 per set bit
-#pragma unroll
-          for (int v = 0; v < 8; v++) r[u][v] = __float_as_uint(__uint_as_float(r[u][v]) * tc::kTwoScale);
+          *reinterpret_cast<float4*>(crow + col) = make_float4(
+              __uint_as_float(r[u][0]), __uint_as_float(r[u][1]), __uint_as_float(r[u][2]), __uint_as_float(r[u][3]));
+          *reinterpret_cast<float4*>(crow + col + 4) = make_float4(
+              __uint_as_float(r[u][4]), __uint_as_float(r[u][5]), __uint_as_float(r[u][6]), __uint_as_float(r[u][7]));
         }
-        *reinterpret_cast<float4*>(crow + col) = make_float4(
-            __uint_as_float(r[u][0]), __uint_as_float(r[u][1]), __uint_as_float(r[u][2]), __uint_as_float(r[u][3]));
-        *reinterpret_cast<float4*>(crow + col + 4) = make_float4(
-            __uint_as_float(r[u][4]), __uint_as_float(r[u][5]), __uint_as_float(r[u][6]), __uint_as_float(r[u][7]));
+        continue;
       }
+      if (!wlive) continue;
+      // the bit operand held 2.0 per set bit; row `lane` of the tile
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        float4* t4 = reinterpret_cast<float4*>(tile + lane * kEpiStride + u * 8);
+        t4[0] = make_float4(__uint_as_float(r[u][0]) * tc::kTwoScale, __uint_as_float(r[u][1]) * tc::kTwoScale,
+                            __uint_as_float(r[u][2]) * tc::kTwoScale, __uint_as_float(r[u][3]) * tc::kTwoScale);
+        t4[1] = make_float4(__uint_as_float(r[u][4]) * tc::kTwoScale, __uint_as_float(r[u][5]) * tc::kTwoScale,
+                            __uint_as_float(r[u][6]) * tc::kTwoScale, __uint_as_float(r[u][7]) * tc::kTwoScale);
+      }
+      __syncwarp();
+      // 8 lanes per row: rows 4*it + lane/8, 16 bytes each
+      const int c4 = (lane & 7) * 4;
+      const int64_t gcol = ccol + c8 * 8 + c4;
+#pragma unroll
+      for (int it = 0; it < 8; it++) {
+        const int j = it * 4 + (lane >> 3);
+        const int64_t grow = rbase + j;
+        if (grow < out_rows && gcol < out_cols)
+          *reinterpret_cast<float4*>(cbase + grow * cld + gcol) =
+              *reinterpret_cast<const float4*>(tile + j * kEpiStride + c4);
+      }
+      __syncwarp();
     }
   }
   ptx::tc_fence_before_sync();
@@ -656,6 +693,8 @@ int make_map(CUtensorMap* m, const void* base, int dt, int64_t rows, int64_t col
 }
 
 static_assert(sizeof(TcSmem) + kSmemAlign <= 232448, "stage ring exceeds the shared memory of a CTA");
+static_assert(kProducerWarps * 32 * kEpiStride * (int)sizeof(float) <= kStages * kStageBytes,
+              "epilogue tiles exceed the stage memory");
 
 template <typename BT, int MODE>
 int launch_mode(const TcArgs& a, const CUtensorMap& ma, const CUtensorMap& mb, dim3 grid, cudaStream_t s) {
