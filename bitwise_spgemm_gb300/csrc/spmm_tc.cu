@@ -48,20 +48,20 @@ constexpr int kHalves = 2;                // a CTA owns two 128-row halves ...
 constexpr int kCtaM = kTcM * kHalves;     // ... 256 output rows, sharing every B tile
 constexpr int kTcN = 256;
 constexpr int kTcK = 32;                  // one packed word of A per row and K tile
-constexpr int kTilesPerStage = 2;         // a stage carries two occupied K tiles
 constexpr int kATile = kCtaM * kTcK * 2;  // 16 KB: both halves of one K tile
 constexpr int kAHalf = kTcM * kTcK * 2;   // 8 KB
 constexpr int kBTile = kTcK * kTcN * 2;   // 16 KB
-constexpr int kStageBytes = kTilesPerStage * kATile;  // per operand: 32 KB
-constexpr int kStages = 3;
+// Each operand has a 96 KB ring of stages.  A stage carries TPS occupied K
+// tiles (a kernel template parameter): 2 tiles in 3 stages of 32 KB, or 3
+// tiles in 2 stages of 48 KB (a third fewer hand-offs per MMA, one stage
+// less in flight).  The SDDMM runs 3 stages of one 32 KB box per operand.
+constexpr int kRingBytes = 96 * 1024;
+constexpr int kMaxStages = 3;
 // Producers: one group of 256 threads (one per row of the CTA tile) per tile
-// of the stage, so a warp expands one tile per stage.
+// of the stage, so a warp expands one tile per stage; then a TMA warp and an
+// MMA warp (allocates TMEM, issues the MMAs).
 constexpr int kGroupThreads = kCtaM;
-constexpr int kProducers = kGroupThreads * kTilesPerStage;
-constexpr int kProducerWarps = kProducers / 32;
-constexpr int kTmaWarp = kProducerWarps;      // issues the TMA boxes
-constexpr int kMmaWarp = kProducerWarps + 1;  // allocates TMEM, issues the MMAs
-constexpr int kTcThreads = kProducers + 64;
+constexpr __host__ __device__ int tc_threads(int tps) { return kGroupThreads * tps + 64; }
 constexpr int kWordAhead = 4;                 // A words are loaded this many stages ahead
 // Occupied K tiles of the CTA, listed once in shared memory: tile index in
 // bits 0-27, which 128-row halves have bits in bits 28-29.
@@ -71,6 +71,7 @@ constexpr uint32_t kTmemCols = 512;       // two 128x256 FP32 accumulators
 // memory, rows 36 floats apart (16-byte aligned; the row-wise float4 writes
 // and the column-block float4 reads are both free of bank conflicts).
 constexpr int kEpiStride = 36;
+constexpr int kEpiWarps = 16;  // 4 TMEM lane quarters x 2 accumulators x 2 column halves
 using tc::kLbo;
 using tc::kSbo;
 using tc::kLayoutSw128;
@@ -83,18 +84,19 @@ constexpr uint32_t kBox = kBoxCols * kTcK * 2;  // 4 KB
 // (256 rows) are one box each, K-major with 128-byte swizzle (rows 128 B,
 // 8-row groups 1 KB apart); the four K=16 steps start 32 B apart.
 constexpr int kSdK = 64;
+constexpr int kSdTile = kCtaM * kSdK * 2;  // one G or X box of a stage: 32 KB
 constexpr uint32_t kSdSbo = 1024;
 // Shared memory is requested with this much slack so the stage buffers can
 // be aligned to the 1 KB swizzle atom.
 constexpr size_t kSmemAlign = 1024;
 
 struct __align__(1024) TcSmem {
-  uint8_t a[kStages][kStageBytes];
-  uint8_t b[kStages][kStageBytes];
+  uint8_t a[kRingBytes];  // stage s at s * stage bytes
+  uint8_t b[kRingBytes];
   int list[kListMax];
   int nlist, seen, lo;
-  uint64_t full[kStages];   // producer warps + the TMA transaction arrival
-  uint64_t empty[kStages];  // tcgen05.commit of the stage's MMAs
+  uint64_t full[kMaxStages];   // producer warps + the TMA transaction arrival
+  uint64_t empty[kMaxStages];  // tcgen05.commit of the stage's MMAs
   uint64_t done;
   uint32_t tmem_addr;
   int abort;
@@ -140,9 +142,17 @@ struct TcArgs {
 // reduction, SBO = 512 B along M/N); the dense 16-bit operands come by TMA
 // in swizzled layouts.  The modes differ only in the producers, the
 // descriptors and the epilogue.
-template <typename BT, int MODE>
-__global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __grid_constant__ CUtensorMap mapA,
-                                                          const __grid_constant__ CUtensorMap mapB) {
+template <typename BT, int MODE, int TPS>
+__global__ void __launch_bounds__(tc_threads(TPS), 1) k_spmm_tc(TcArgs a, const __grid_constant__ CUtensorMap mapA,
+                                                               const __grid_constant__ CUtensorMap mapB) {
+  constexpr int kTilesPerStage = TPS;
+  constexpr int kStageBytes = MODE == kSddmm ? kSdTile : TPS * kATile;
+  constexpr int kStages = kRingBytes / kStageBytes;
+  constexpr int kProducerWarps = kGroupThreads * TPS / 32;
+  constexpr int kTmaWarp = kProducerWarps;
+  constexpr int kMmaWarp = kProducerWarps + 1;
+  static_assert(kStages >= 2 && kStages <= kMaxStages, "stage ring");
+  static_assert(kProducerWarps >= kEpiWarps, "the epilogue runs on producer warps");
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   TcSmem& sm = *reinterpret_cast<TcSmem*>(
       smem_raw + ((kSmemAlign - (ptx::smem_addr(smem_raw) & (kSmemAlign - 1))) & (kSmemAlign - 1)));
@@ -308,7 +318,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
         }
         if (!__shfl_sync(kFull, go, 0)) break;
         if (kTilesPerStage * i + u < n) {
-          uint8_t* at = sm.a[s] + u * kATile;
+          uint8_t* at = sm.a + s * kStageBytes + u * kATile;
           uint4 e[4];
           tc::expand32_two(w0, e);
           if (kFwdLike) {
@@ -335,7 +345,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
   } else if (warp == kTmaWarp && lane == 0) {
     // ---------------- TMA issuer ----------------
     // Shared-memory addresses are formed once; a stage adds its offset.
-    const uint32_t a0 = ptx::smem_addr(sm.a[0]), b0 = ptx::smem_addr(sm.b[0]), f0 = ptx::smem_addr(&sm.full[0]);
+    const uint32_t a0 = ptx::smem_addr(sm.a), b0 = ptx::smem_addr(sm.b), f0 = ptx::smem_addr(&sm.full[0]);
     if (MODE == kBatch) ptx::tensormap_acquire(bmap);  // written by the host into global memory
     for (int i = 0; i < nstages; i++) {
       const int s = i % kStages;
@@ -347,33 +357,32 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
       const uint32_t fb = f0 + s * 8, as = a0 + s * kStageBytes, bs = b0 + s * kStageBytes;
       if (MODE == kSddmm) {
         // G rows row0.. and X rows col0.. (256 each), N columns i*64..
-        ptx::mbar_arrive_expect_tx(&sm.full[s], 2 * kStageBytes);
+        ptx::mbar_arrive_expect_tx(&sm.full[s], 2 * kSdTile);
         ptx::tma_load_2d_u32(as, &mapA, i * kSdK, (int)row0, fb);
         ptx::tma_load_2d_u32(bs, &mapB, i * kSdK, (int)col0, fb);
       } else {
         // B (fwd) / G (trans) rows t*32.. of the stage's tiles, columns col0 + 64*j
         const int k0 = kTilesPerStage * i;
-        const bool two = k0 + 1 < n;
-        const int t0 = lst[k0] & 0x0fffffff;
-        ptx::mbar_arrive_expect_tx(&sm.full[s], (two ? 2 : 1) * nbox * kBox);
+        const int cnt = min(kTilesPerStage, n - k0);  // tiles in this stage
+        ptx::mbar_arrive_expect_tx(&sm.full[s], cnt * nbox * kBox);
         if (MODE != kBatch && a.bt) {
-          // tiled B: the tile's first nbox atoms are one contiguous copy
-          const uint8_t* src = a.bt + ((int64_t)t0 * a.bt_cb + blockIdx.y) * kBTile;
-          ptx::bulk_g2s(sm.b[s], src, nbox * kBox, &sm.full[s]);
-          if (two)
-            ptx::bulk_g2s(sm.b[s] + kBTile, a.bt + ((int64_t)(lst[k0 + 1] & 0x0fffffff) * a.bt_cb + blockIdx.y) * kBTile,
-                          nbox * kBox, &sm.full[s]);
+          // tiled B: each tile's first nbox atoms are one contiguous copy
+#pragma unroll
+          for (int u = 0; u < kTilesPerStage; u++)
+            if (u < cnt)
+              ptx::bulk_g2s(sm.b + s * kStageBytes + u * kBTile,
+                            a.bt + ((int64_t)(lst[k0 + u] & 0x0fffffff) * a.bt_cb + blockIdx.y) * kBTile,
+                            nbox * kBox, &sm.full[s]);
           continue;
         }
 #pragma unroll
-        for (int j = 0; j < kTcN / kBoxCols; j++)
-          if (j < nbox) ptx::tma_load_2d_u32(bs + j * kBox, bmap, (int)col0 + j * kBoxCols, t0 * kTcK, fb);
-        if (two) {
-          const int t1 = lst[k0 + 1] & 0x0fffffff;
+        for (int u = 0; u < kTilesPerStage; u++) {
+          if (u >= cnt) break;
+          const int t = lst[k0 + u] & 0x0fffffff;
 #pragma unroll
           for (int j = 0; j < kTcN / kBoxCols; j++)
             if (j < nbox)
-              ptx::tma_load_2d_u32(bs + kBTile + j * kBox, bmap, (int)col0 + j * kBoxCols, t1 * kTcK, fb);
+              ptx::tma_load_2d_u32(bs + u * kBTile + j * kBox, bmap, (int)col0 + j * kBoxCols, t * kTcK, fb);
         }
       }
     }
@@ -384,7 +393,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
     const uint32_t ab = std::is_same<BT, __nv_bfloat16>::value ? 1u : 0u;
     const uint32_t idesc = tc::idesc_f16(ab, MODE == kTrans ? 1u : 0u, MODE == kSddmm ? 0u : 1u,
                                          (uint32_t)(nbox * kBoxCols), kTcM);
-    const uint32_t a0 = ptx::smem_addr(sm.a[0]), b0 = ptx::smem_addr(sm.b[0]);
+    const uint32_t a0 = ptx::smem_addr(sm.a), b0 = ptx::smem_addr(sm.b);
     const uint64_t adesc = MODE == kSddmm ? ptx::smem_desc_noswizzle_u32(a0, 16, kSdSbo) | ((uint64_t)kLayoutSw128 << 61)
                                           : ptx::smem_desc_noswizzle_u32(a0, kLbo, kSbo);
     const uint64_t bdesc = MODE == kSddmm ? ptx::smem_desc_noswizzle_u32(b0, 16, kSdSbo) | ((uint64_t)kLayoutSw128 << 61)
@@ -393,23 +402,25 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
     // cycle this thread spends between stages is idle tensor time: the next
     // stage's halves are read from the list while this stage issues, and the
     // abort flag is not polled here either.
-    auto halves = [&](int st, int& h0, int& h1) {
-      h0 = dense_halves;
-      h1 = 0;
-      if (MODE != kSddmm && st < nstages) {
-        const int k0 = kTilesPerStage * st;
-        h0 = (lst[k0] >> 28) & 3;
-        h1 = k0 + 1 < n ? (lst[k0 + 1] >> 28) & 3 : 0;
+    auto halves = [&](int st, int (&hv)[kTilesPerStage]) {
+#pragma unroll
+      for (int u = 0; u < kTilesPerStage; u++) {
+        const int k = kTilesPerStage * st + u;
+        hv[u] = MODE == kSddmm ? (u == 0 ? dense_halves : 0)
+                               : (st < nstages && k < n ? (lst[k] >> 28) & 3 : 0);
       }
     };
     uint32_t started = 0;
     int i = 0;
-    int hn0, hn1;
-    halves(0, hn0, hn1);
+    int hn[kTilesPerStage];
+    halves(0, hn);
     for (; i < nstages; i++) {
       const int s = i % kStages;
-      const int hv0 = hn0, hv1 = hn1;
-      halves(i + 1, hn0, hn1);
+      int hv[kTilesPerStage];
+#pragma unroll
+      for (int u = 0; u < kTilesPerStage; u++) hv[u] = hn[u];
+      halves(i + 1, hn);
+      const int hv0 = hv[0];
       if (!ptx::mbar_wait(&sm.full[s], (i / kStages) & 1)) {
         atomicCAS(&g_tc_error, 0, 3);
         sm.abort = 1;
@@ -431,10 +442,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
       } else {
 #pragma unroll
         for (int u = 0; u < kTilesPerStage; u++) {
-          const int hv = u == 0 ? hv0 : hv1;
+          const int hu = hv[u];
 #pragma unroll
           for (int h = 0; h < kHalves; h++) {
-            if (!((hv >> h) & 1)) continue;
+            if (!((hu >> h) & 1)) continue;
 #pragma unroll
             for (int j = 0; j < 2; j++)  // K half j: A two core-matrix columns on, B two 8-row groups on
               ptx::tc_mma_f16(tmem + (uint32_t)(h * kTcN),
@@ -457,7 +468,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
   // than the SDDMM pass them through a 32x32 tile of the (now idle) stage
   // memory, so that each store instruction writes four whole 128-byte rows
   // of C instead of 16 bytes in each of 32 rows.
-  if (warp < kProducerWarps) {
+  if (warp < kEpiWarps) {
     const int h = (warp >> 2) & 1, q = warp & 3, cg = warp >> 3;
     const bool have = (sm.seen >> h) & 1;
     // warp-uniform flags: the TMEM loads and the tile hand-off below are
@@ -478,7 +489,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spmm_tc(TcArgs a, const __gri
     const bool live = row < out_rows && wlive;
     const uint32_t* arow = gA + row * gKw;
     const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * kTcN + cg * (kTcN / 2));
-    float* tile = reinterpret_cast<float*>(sm.a[0]) + warp * 32 * kEpiStride;
+    float* tile = reinterpret_cast<float*>(sm.a) + warp * 32 * kEpiStride;
     // columns of this warp's half that hold output: up to 64·nbox of the tile
     const int c8_end = (int)max(0, min(kTcN / 2, nbox * kBoxCols - cg * (kTcN / 2))) / 8;
     for (int c8 = 0; c8 < c8_end; c8 += 4) {
@@ -693,20 +704,20 @@ int make_map(CUtensorMap* m, const void* base, int dt, int64_t rows, int64_t col
 }
 
 static_assert(sizeof(TcSmem) + kSmemAlign <= 232448, "stage ring exceeds the shared memory of a CTA");
-static_assert(kProducerWarps * 32 * kEpiStride * (int)sizeof(float) <= kStages * kStageBytes,
+static_assert(kEpiWarps * 32 * kEpiStride * (int)sizeof(float) <= kRingBytes,
               "epilogue tiles exceed the stage memory");
 
-template <typename BT, int MODE>
+template <typename BT, int MODE, int TPS>
 int launch_mode(const TcArgs& a, const CUtensorMap& ma, const CUtensorMap& mb, dim3 grid, cudaStream_t s) {
   const size_t smem = sizeof(TcSmem) + kSmemAlign;
   static bool configured[64] = {};
   int dev = 0;
   BSP_CUDA(cudaGetDevice(&dev));
   if (dev < 64 && !configured[dev]) {
-    BSP_CUDA(cudaFuncSetAttribute(k_spmm_tc<BT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    BSP_CUDA(cudaFuncSetAttribute(k_spmm_tc<BT, MODE, TPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     configured[dev] = true;
   }
-  k_spmm_tc<BT, MODE><<<grid, kTcThreads, smem, s>>>(a, ma, mb);
+  k_spmm_tc<BT, MODE, TPS><<<grid, tc_threads(TPS), smem, s>>>(a, ma, mb);
   BSP_LAUNCHED();
   return BSP_OK;
 }
@@ -771,6 +782,18 @@ size_t tc_preferred_bytes(int64_t out_rows, int64_t out_cols, int64_t red_rows) 
 
 namespace {
 
+// Three K tiles per stage (two stages) where the output has this many row
+// blocks; BSP_TC_TPS=2 or 3 forces one form.
+constexpr int64_t kThreeTileMinRowBlocks = 32;
+bool three_tiles(int64_t out_rows) {
+  static const int force = [] {
+    const char* e = getenv("BSP_TC_TPS");
+    return e && *e ? atoi(e) : 0;
+  }();
+  if (force == 2 || force == 3) return force == 3;
+  return ceil_div(out_rows, kCtaM) >= kThreeTileMinRowBlocks;
+}
+
 // BSP_TC_TILED_B=0 keeps B on tensor boxes even with room for the tiled copy.
 bool tiled_b_enabled() {
   static const bool on = [] {
@@ -829,9 +852,19 @@ int launch_tc(TcArgs a, cudaStream_t s, void* ws = nullptr, size_t ws_bytes = 0)
     a.bt = bt;
     a.bt_cb = ncb;
   }
-  if (a.bdt == BSP_BF16) BSP_TRY((launch_mode<__nv_bfloat16, MODE>(a, ma, mb, grid, s)));
-  else if (a.bdt == BSP_F16) BSP_TRY((launch_mode<__half, MODE>(a, ma, mb, grid, s)));
-  else return BSP_ERR_UNSUPPORTED;
+  if (a.bdt != BSP_BF16 && a.bdt != BSP_F16) return BSP_ERR_UNSUPPORTED;
+  bool launched = false;
+  if constexpr (MODE != kSddmm) {  // (the SDDMM has one stage form)
+    if (three_tiles(rows)) {
+      if (a.bdt == BSP_BF16) BSP_TRY((launch_mode<__nv_bfloat16, MODE, 3>(a, ma, mb, grid, s)));
+      else BSP_TRY((launch_mode<__half, MODE, 3>(a, ma, mb, grid, s)));
+      launched = true;
+    }
+  }
+  if (!launched) {
+    if (a.bdt == BSP_BF16) BSP_TRY((launch_mode<__nv_bfloat16, MODE, 2>(a, ma, mb, grid, s)));
+    else BSP_TRY((launch_mode<__half, MODE, 2>(a, ma, mb, grid, s)));
+  }
   if (splits > 1) {
     const int64_t work = rows * (cols / 4);
     const int64_t cap = (int64_t)num_sms() * 8;
@@ -915,8 +948,8 @@ int launch_batched_tc(const BatchProblemTc* probs, const int4* items, int n_item
   CUtensorMap unused;
   memset(&unused, 0, sizeof(unused));
   const dim3 grid((unsigned)n_items, 1, 1);
-  if (bdt == BSP_BF16) return launch_mode<__nv_bfloat16, kBatch>(a, unused, unused, grid, s);
-  if (bdt == BSP_F16) return launch_mode<__half, kBatch>(a, unused, unused, grid, s);
+  if (bdt == BSP_BF16) return launch_mode<__nv_bfloat16, kBatch, 2>(a, unused, unused, grid, s);
+  if (bdt == BSP_F16) return launch_mode<__half, kBatch, 2>(a, unused, unused, grid, s);
   return BSP_ERR_UNSUPPORTED;
 }
 

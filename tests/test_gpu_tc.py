@@ -175,3 +175,24 @@ def _t_workspaces(M, K, N):
     capi.call("bsp_spmm_t_workspace_preferred", M, K, N, ctypes.byref(b))
     assert b.value >= a.value
     return a.value, b.value
+
+
+@pytest.mark.parametrize("kind", ["bf16", "f16"])
+@pytest.mark.parametrize("M,K,N,p", [(8200, 1000, 264, 0.05), (8448, 3000, 64, 0.01)])
+def test_three_tile_stages(force_tc, kind, M, K, N, p):
+    # 32+ row blocks: stages of three K tiles (two stages in flight); list
+    # lengths that are not multiples of three leave a short last stage
+    rng = np.random.default_rng(M + K)
+    bits = rng.random((M, K)) < p
+    bits[:300, 96:320] = False  # a run of empty K tiles for the first row blocks
+    words = W.pack_bits(bits)
+    wd = words_dev(words)
+    plan = ops.Plan(wd, K)
+    Bi, Bie = _b16(rng.integers(-8, 9, (K, N)).astype(np.float32), kind)
+    C = ops.spmm(wd, K, Bi, plan=plan).cpu().numpy()
+    assert capi.device_status() == 0
+    assert np.array_equal(C.astype(np.float64), O.spmm_f64(words, K, Bie))
+    B, Bexact = _b16(rng.standard_normal((K, N)).astype(np.float32), kind)
+    C = ops.spmm(wd, K, B, plan=plan).cpu().numpy()
+    mx, _, _ = O.rel_errors(C, O.spmm_f64(words, K, Bexact), O.spmm_abs_f64(words, K, Bexact))
+    assert mx <= TOL
