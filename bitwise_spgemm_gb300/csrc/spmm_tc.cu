@@ -10,22 +10,26 @@
 // CTA tile: 256 rows x 256 columns of C as two 128-row halves, each with its
 // FP32 accumulator in TMEM (2 x 256 columns); both halves multiply the same
 // B stage, so every B byte brought into shared memory feeds 256 rows.  K
-// advances 32 columns (one packed word) per stage, over the K tiles where
-// either 128-row block has a set bit (the plan's occupancy bitmap, one per
-// 128-row block); a half without bits in the tile skips its MMAs.
-//   warps 0-7 (A producers): expand the words of the stage's two K tiles
-//     into the A operand (K-major core-matrix layout, one row per thread);
-//     after the last stage they read the accumulators back with tcgen05.ld
-//     and store C;
-//   warp 8 (TMA): issues the B rows of the stage's tiles as 64x32 boxes in
-//     the 128-byte-swizzled MN-major layout;
-//   warp 9: allocates TMEM; its lane 0 issues two tcgen05.mma (K=16) per
+// advances over the 32-column tiles where either 128-row block has a set bit
+// (the plan's occupancy bitmap); a half without bits in a tile skips its
+// MMAs.  A stage carries TPS tiles (2 tiles x 3 stages, or 3 x 2 where many
+// row blocks share B); per CTA:
+//   256·TPS producer threads (one row of one tile each): load the tile's
+//     words (column-major copy in the plan: one 128-byte run per warp),
+//     expand them into the A operand (K-major core matrices, 2.0 per set
+//     bit) and arrive on the stage's "full" mbarrier; after the last stage
+//     16 of these warps read the accumulators back (tcgen05.ld), scale by
+//     0.5 and store C through a 32x32 staging tile per warp;
+//   a TMA warp: B rows of the stage's tiles, either as one bulk copy of 16
+//     KB per tile from B already in tile order (k_tile_b) or as four 64x32
+//     tensor boxes (128-byte swizzle, MN-major);
+//   an MMA warp: allocates TMEM; its lane 0 issues two tcgen05.mma (K=16) per
 //     occupied half per tile and commits the stage to its "empty" mbarrier.
-// An mbarrier hand-off costs 200-400 cycles on GB300 whatever the waiting
-// form, so a stage carries two tiles (up to eight MMAs, ~1000 cycles of
-// tensor work) per wait and per commit.  Three stages of 64 KB; every
-// mbarrier wait is bounded (timeout → error 3 in g_tc_error, the CTA skips to
-// freeing its TMEM).
+// An mbarrier hand-off costs 200-500 cycles on GB300, and the tensor pipe
+// queues about one MMA beyond the running one, so the design keeps the
+// MMA thread's work between stages minimal and carries several tiles per
+// hand-off.  Every mbarrier wait is bounded (timeout -> error 3 in
+// g_tc_error, the CTA skips its stores and frees its TMEM).
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
