@@ -68,6 +68,7 @@ SIGNATURES = {
     "bsp_group_to_dense": [_P, _P, _P, _I64, _I64, _I, _I, _P, _I64, _P],
     "bsp_plan_create": [_P, _I64, _I64, C.POINTER(PlanParams), C.POINTER(_P), _P],
     "bsp_plan_destroy": [_P],
+    "bsp_plan_destroy_async": [_P, _P],
     "bsp_plan_get_info": [_P, C.POINTER(PlanInfo)],
     "bsp_spmm_workspace": [_P, _I64, C.POINTER(_SZ)],
     "bsp_spmm": [_P, _I64, _I64, _P, _I, _I64, _I64, _P, _I64, _P, _P, _SZ, _P],

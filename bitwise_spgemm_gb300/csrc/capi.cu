@@ -199,6 +199,13 @@ int bsp_plan_destroy(bsp_plan* plan) {
   return BSP_OK;
 }
 
+int bsp_plan_destroy_async(bsp_plan* plan, bsp_stream_t stream) {
+  if (!plan) return BSP_OK;
+  const int st = plan_free_async(plan, (cudaStream_t)stream);
+  delete plan;
+  return st;
+}
+
 int bsp_plan_get_info(const bsp_plan* plan, bsp_plan_info* info) {
   if (!plan || !info) return BSP_ERR_INVALID_ARG;
   info->M = plan->M;

@@ -181,6 +181,37 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_apply(const int32_t* __re
   }
 }
 
+// Small inputs: one CTA walks the tiles in order with a running carry, so
+// the scan is one launch instead of three.
+constexpr int kScanSingleThreads = 1024;
+constexpr int64_t kScanSingleMax = 32768;
+__global__ void __launch_bounds__(kScanSingleThreads) k_scan_single(const int32_t* __restrict__ in, int64_t n,
+                                                                    int32_t* __restrict__ out) {
+  __shared__ int sw[32];
+  constexpr int TILE = kScanSingleThreads * kScanItems;
+  int carry = 0;
+  for (int64_t base = 0; base < n; base += TILE) {
+    int v[kScanItems];
+    int s = 0;
+#pragma unroll
+    for (int j = 0; j < kScanItems; j++) {
+      const int64_t i = base + (int64_t)threadIdx.x * kScanItems + j;
+      v[j] = i < n ? in[i] : 0;
+      s += v[j];
+    }
+    int total;
+    int run = block_exclusive_scan(s, sw, &total) + carry;
+#pragma unroll
+    for (int j = 0; j < kScanItems; j++) {
+      const int64_t i = base + (int64_t)threadIdx.x * kScanItems + j;
+      if (i < n) out[i] = run;
+      run += v[j];
+    }
+    carry += total;
+  }
+  if (threadIdx.x == 0) out[n] = carry;
+}
+
 int grid_for(int64_t warps_needed) {
   const int64_t blocks = ceil_div(warps_needed, 8);
   const int64_t cap = (int64_t)num_sms() * 16;
@@ -223,6 +254,11 @@ int launch_scan_i32(const int32_t* in, int64_t n, int32_t* out, void* ws, cudaSt
   const int64_t nb = ceil_div(n, kScanTile);
   if (nb == 0) {
     BSP_CUDA(cudaMemsetAsync(out, 0, sizeof(int32_t), s));
+    return BSP_OK;
+  }
+  if (n <= kScanSingleMax) {
+    k_scan_single<<<1, kScanSingleThreads, 0, s>>>(in, n, out);
+    BSP_LAUNCHED();
     return BSP_OK;
   }
   int32_t* bsum = static_cast<int32_t*>(ws);

@@ -6,7 +6,8 @@
 // clustered row, only the bits where it differs from its cluster's majority
 // mask ("consensus"), so the SpMM adds ~16 rows of B per row instead of ~420.
 //
-// Steps (all on the GPU, one stream; the host reads back three counters):
+// Steps (all on the GPU, on the caller's stream; the host reads back the
+// cluster count and the plan's counters to size buffers):
 //  1. signatures: H MinHash values per row — h_j(row) = min over the row's
 //     set columns k of mix(k, j) — plus the row's popcount (warp per row,
 //     __popc + warp min-reduction);
@@ -28,7 +29,9 @@
 //     delta lists (ascending column, bit 31 = column present in the consensus
 //     but not in the row → subtract) are laid out by an exclusive scan.
 // Every step is order-independent or ordered by row index, so the plan is a
-// deterministic function of A.
+// deterministic function of A.  The tensor-core structures (occupancy bitmaps,
+// A's words by column) depend on A alone and are built on a side stream
+// meanwhile.
 #include <climits>
 #include <mutex>
 #include <cstdlib>
@@ -71,7 +74,29 @@ __device__ __forceinline__ uint32_t slot_of(uint32_t key, uint32_t mask) {
   return (key * 0x9e3779b1u) & mask;
 }
 
-// Warp per row: H MinHash values and the popcount.
+// Position of the n-th (0-based) set bit of x; n < popcount(x).
+__device__ __forceinline__ int nth_set_bit(uint32_t x, int n) {
+  int pos = 0;
+#pragma unroll
+  for (int width = 16; width; width >>= 1) {
+    const uint32_t low = x & ((1u << width) - 1u);
+    const int c = __popc(low);
+    if (n >= c) {
+      n -= c;
+      x >>= width;
+      pos += width;
+    } else {
+      x = low;
+    }
+  }
+  return pos;
+}
+
+// Warp per row: H MinHash values and the popcount.  The row's words are taken
+// 32 at a time (one per lane) and their set bits are dealt out evenly: lane l
+// takes bits l, l+32, ... of the group in column order (its source word found
+// by a binary search over the lanes' inclusive bit counts), so every lane
+// hashes about the same number of columns however the bits fall.
 __global__ void __launch_bounds__(256) k_signatures(const uint32_t* __restrict__ words, int64_t M,
                                                     int Kw, int H, uint32_t seed,
                                                     uint32_t* __restrict__ sig,
@@ -84,16 +109,34 @@ __global__ void __launch_bounds__(256) k_signatures(const uint32_t* __restrict__
   for (int j = 0; j < kMaxHashes; j++) mn[j] = kEmpty;
   int cnt = 0;
   const uint32_t* r = words + row * Kw;
-  for (int w = lane; w < Kw; w += 32) {
-    uint32_t x = __ldg(r + w);
-    cnt += __popc(x);
-    while (x) {
-      const int b = __ffs(x) - 1;
-      x &= x - 1;
-      const uint32_t k = (uint32_t)(w * 32 + b);
+  for (int g = 0; g < Kw; g += 32) {
+    const uint32_t x = (g + lane < Kw) ? __ldg(r + g + lane) : 0u;
+    const int c = __popc(x);
+    int incl = c;
 #pragma unroll
-      for (int j = 0; j < kMaxHashes; j++)
-        if (j < H) mn[j] = min(mn[j], mix32(k, (uint32_t)j, seed));
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(kFull, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const int excl = incl - c;
+    const int total = __shfl_sync(kFull, incl, 31);
+    cnt += total;
+    for (int b0 = 0; b0 < total; b0 += 32) {
+      const int gi = b0 + lane;  // this lane's bit of the group, in column order
+      int src = 0;               // lanes whose words end before bit gi
+#pragma unroll
+      for (int step = 16; step; step >>= 1) {
+        const int v = __shfl_sync(kFull, incl, src + step - 1);
+        if (v <= gi) src += step;
+      }
+      const uint32_t wx = __shfl_sync(kFull, x, src);
+      const int ex = __shfl_sync(kFull, excl, src);
+      if (gi < total) {
+        const uint32_t k = (uint32_t)((g + src) * 32 + nth_set_bit(wx, gi - ex));
+#pragma unroll
+        for (int j = 0; j < kMaxHashes; j++)
+          if (j < H) mn[j] = min(mn[j], mix32(k, (uint32_t)j, seed));
+      }
     }
   }
 #pragma unroll
@@ -102,7 +145,6 @@ __global__ void __launch_bounds__(256) k_signatures(const uint32_t* __restrict__
     const uint32_t m = __reduce_min_sync(kFull, mn[j]);
     if (lane == j) sig[row * H + j] = m;
   }
-  cnt = __reduce_add_sync(kFull, (unsigned)cnt);
   if (lane == 0) nnz[row] = cnt;
 }
 
@@ -397,13 +439,61 @@ struct DevBuf {
 inline size_t al256(size_t b) { return (b + 255) & ~size_t(255); }
 
 // The plan's own storage, from the same pool (the plan is synchronised with
-// its stream before it is returned, so any stream may use it afterwards);
-// bsp_plan_destroy's cudaFree waits for the device and returns it there.
-cudaError_t plan_alloc(void** p, size_t bytes, cudaStream_t s) {
+// its stream before it is returned, so any stream may use it afterwards).
+// *pooled tells the destroy calls whether the block goes back with
+// cudaFree (waits for the device) or may go back in stream order.
+cudaError_t plan_alloc(void** p, size_t bytes, cudaStream_t s, bool* pooled) {
   cudaMemPool_t pool = temp_pool();
-  if (pool && cudaMallocFromPoolAsync(p, bytes, pool, s) == cudaSuccess) return cudaSuccess;
+  *pooled = pool && cudaMallocFromPoolAsync(p, bytes, pool, s) == cudaSuccess;
+  if (*pooled) return cudaSuccess;
   return cudaMalloc(p, bytes);
 }
+
+// A non-blocking stream per device for plan-build work that the grouping does
+// not wait on (the tensor-core structures); created once, kept until exit.
+cudaStream_t side_stream() {
+  static std::mutex mu;
+  static cudaStream_t streams[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> lk(mu);
+  if (!streams[dev] && cudaStreamCreateWithFlags(&streams[dev], cudaStreamNonBlocking) != cudaSuccess)
+    streams[dev] = nullptr;
+  return streams[dev];
+}
+
+// Work forked from stream `s` onto the side stream: join() makes `s` wait for
+// it; the destructor joins too (and frees the events), so temporaries that
+// are freed on `s` afterwards outlive the side work on every return path.
+struct SideFork {
+  cudaStream_t s = nullptr, side = nullptr;
+  cudaEvent_t fork = nullptr, done = nullptr;
+  bool joined = true;
+  int start(cudaStream_t main) {
+    s = main;
+    side = side_stream();
+    if (!side) return BSP_OK;  // no side stream: the work runs on `s`
+    BSP_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+    BSP_CUDA(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
+    BSP_CUDA(cudaEventRecord(fork, s));
+    BSP_CUDA(cudaStreamWaitEvent(side, fork, 0));
+    joined = false;
+    return BSP_OK;
+  }
+  cudaStream_t stream() const { return side ? side : s; }
+  int join() {
+    if (joined) return BSP_OK;
+    joined = true;
+    BSP_CUDA(cudaEventRecord(done, side));
+    BSP_CUDA(cudaStreamWaitEvent(s, done, 0));
+    return BSP_OK;
+  }
+  ~SideFork() {
+    join();
+    if (fork) cudaEventDestroy(fork);
+    if (done) cudaEventDestroy(done);
+  }
+};
 
 }  // namespace
 
@@ -451,6 +541,27 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
   BSP_CUDA(cudaMemsetAsync(lead, 0x7f, sizeof(int32_t) * tsize, s));
   BSP_CUDA(cudaMemsetAsync(stats, 0, sizeof(unsigned long long) * 8, s));
 
+  // ---- tensor-core structures: occupancy bitmaps and A's words by column
+  // (the producers then load the words of 32 consecutive rows or columns as
+  // one 128-byte run).  They depend on A only, so they are built on a side
+  // stream while the grouping below runs; their tile counts land in stats[5],
+  // stats[6] before the stats are read.
+  size_t qoff = 0;
+  auto qtake = [&](size_t bytes) { const size_t o = qoff; qoff += al256(bytes); return o; };
+  const size_t p_occ = qtake(sizeof(uint32_t) * ceil_div(M, 128) * tc_occupancy_words(K));
+  const size_t p_occT = qtake(sizeof(uint32_t) * ceil_div(K, 128) * tc_occupancy_t_words(M));
+  const bool with_wt = (double)M * (double)Kw * 4.0 <= (double)(1ull << 32) && ceil_div(M, 32) <= 65535;
+  const size_t p_wt = qtake(with_wt ? sizeof(uint32_t) * (size_t)Kw * (size_t)M : 0);
+  BSP_CUDA(plan_alloc(&plan->tc_arena, qoff, s, &plan->tc_pooled));
+  char* Qa = static_cast<char*>(plan->tc_arena);
+  plan->occ = (uint32_t*)(Qa + p_occ);
+  plan->occT = (uint32_t*)(Qa + p_occT);
+  plan->wordsT = with_wt ? (uint32_t*)(Qa + p_wt) : nullptr;
+  SideFork tc;
+  BSP_TRY(tc.start(s));
+  BSP_TRY(launch_occupancy(words, M, K, plan->occ, plan->occT, stats + 5, stats + 6, tc.stream()));
+  if (with_wt) BSP_TRY(launch_transpose_words(words, M, Kw, plan->wordsT, tc.stream()));
+
   const unsigned wgrid = (unsigned)ceil_div(M, 8);    // warp-per-row kernels, 256 threads
   const unsigned tgrid = (unsigned)ceil_div(M, 256);  // thread-per-row kernels
   k_signatures<<<wgrid, 256, 0, s>>>(words, M, Kw, H, prm->seed, sig, nnz);
@@ -475,27 +586,14 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
   const size_t p_dp = ptake(sizeof(int32_t) * (M + 1));
   const size_t p_cons = ptake(sizeof(uint32_t) * ncl * Kw);
   const size_t p_dl = ptake(sizeof(int32_t) * M);
-  const size_t p_occ = ptake(sizeof(uint32_t) * ceil_div(M, 128) * tc_occupancy_words(K));
-  const size_t p_occT = ptake(sizeof(uint32_t) * ceil_div(K, 128) * tc_occupancy_t_words(M));
-  // A's words by column: the tensor-core producers then load the words of
-  // 32 consecutive rows (forward) or columns (transposed) as one 128-byte run
-  const bool with_wt = (double)M * (double)Kw * 4.0 <= (double)(1ull << 32) && ceil_div(M, 32) <= 65535;
-  const size_t p_wt = ptake(with_wt ? sizeof(uint32_t) * (size_t)Kw * (size_t)M : 0);
   void* parena = nullptr;
-  BSP_CUDA(plan_alloc(&parena, poff ? poff : 16, s));
+  BSP_CUDA(plan_alloc(&parena, poff ? poff : 16, s, &plan->arena_pooled));
   plan->arena = parena;
   char* Pa = static_cast<char*>(parena);
   plan->row_cluster = (int32_t*)(Pa + p_cl);
   plan->delta_ptr = (int32_t*)(Pa + p_dp);
   plan->cons = (uint32_t*)(Pa + p_cons);
   plan->direct_list = (int32_t*)(Pa + p_dl);
-  plan->occ = (uint32_t*)(Pa + p_occ);
-  plan->occT = (uint32_t*)(Pa + p_occT);
-  BSP_TRY(launch_occupancy(words, M, K, plan->occ, plan->occT, stats + 5, stats + 6, s));
-  if (with_wt) {
-    plan->wordsT = (uint32_t*)(Pa + p_wt);
-    BSP_TRY(launch_transpose_words(words, M, Kw, plan->wordsT, s));
-  }
   plan->n_proto = ncl;
 
   if (ncl > 0) {
@@ -534,7 +632,6 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
                                           asize - 1, plan->row_cluster, dcnt, stats);
     k_cons_popc<<<(unsigned)ceil_div(ncl * Kw, 256), 256, 0, s>>>(plan->cons, ncl * Kw, stats);
     BSP_LAUNCHED();
-    BSP_CUDA(cudaStreamSynchronize(s));  // t2 is freed on scope exit
   } else {
     BSP_CUDA(cudaMemsetAsync(plan->row_cluster, 0xff, sizeof(int32_t) * M, s));
     BSP_CUDA(cudaMemsetAsync(dcnt, 0, sizeof(int32_t) * M, s));
@@ -544,6 +641,7 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
   }
   BSP_TRY(launch_scan_i32(dcnt, M, plan->delta_ptr, scanws, s));
   unsigned long long st[8];
+  BSP_TRY(tc.join());
   BSP_CUDA(cudaMemcpyAsync(st, stats, sizeof(st), cudaMemcpyDeviceToHost, s));
   BSP_CUDA(cudaStreamSynchronize(s));
   plan->nnz = (int64_t)st[0];
@@ -571,7 +669,7 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
     BSP_LAUNCHED();
   }
   if (mode == BSP_PLAN_PROTO && plan->delta_nnz > 0) {
-    BSP_CUDA(plan_alloc(&plan->delta_arena, sizeof(uint32_t) * plan->delta_nnz, s));
+    BSP_CUDA(plan_alloc(&plan->delta_arena, sizeof(uint32_t) * plan->delta_nnz, s, &plan->delta_pooled));
     plan->delta_idx = (uint32_t*)plan->delta_arena;
     k_delta_fill<<<wgrid, 256, 0, s>>>(words, M, Kw, plan->cons, plan->row_cluster,
                                        plan->delta_ptr, plan->delta_idx);
@@ -584,7 +682,21 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
 void plan_free(bsp_plan* plan) {
   if (plan->arena) cudaFree(plan->arena);
   if (plan->delta_arena) cudaFree(plan->delta_arena);
-  plan->arena = plan->delta_arena = nullptr;
+  if (plan->tc_arena) cudaFree(plan->tc_arena);
+  plan->arena = plan->delta_arena = plan->tc_arena = nullptr;
+}
+
+int plan_free_async(bsp_plan* plan, cudaStream_t s) {
+  void** blocks[3] = {&plan->arena, &plan->delta_arena, &plan->tc_arena};
+  const bool pooled[3] = {plan->arena_pooled, plan->delta_pooled, plan->tc_pooled};
+  int st = BSP_OK;
+  for (int i = 0; i < 3; i++) {
+    if (!*blocks[i]) continue;
+    const cudaError_t e = pooled[i] ? cudaFreeAsync(*blocks[i], s) : cudaFree(*blocks[i]);
+    if (e != cudaSuccess && st == BSP_OK) st = cuda_status(e);
+    *blocks[i] = nullptr;
+  }
+  return st;
 }
 
 }  // namespace bsp

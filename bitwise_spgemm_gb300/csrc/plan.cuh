@@ -10,6 +10,8 @@ struct bsp_plan {
   // device storage (owned)
   void* arena = nullptr;        // row_cluster, delta_ptr, cons
   void* delta_arena = nullptr;  // delta_idx
+  void* tc_arena = nullptr;     // occ, occT, wordsT
+  bool arena_pooled = false, delta_pooled = false, tc_pooled = false;  // from the stream-ordered pool
   int32_t* row_cluster = nullptr;
   int32_t* delta_ptr = nullptr;
   uint32_t* delta_idx = nullptr;
@@ -26,4 +28,6 @@ namespace bsp {
 int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_params* prm,
                bsp_plan* plan, cudaStream_t s);
 void plan_free(bsp_plan* plan);
+// Returns pooled blocks in stream order on s (other blocks with cudaFree).
+int plan_free_async(bsp_plan* plan, cudaStream_t s);
 }  // namespace bsp

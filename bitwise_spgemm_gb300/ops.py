@@ -148,6 +148,13 @@ class Plan:
             self._lib.bsp_plan_destroy(self._h)
             self._h = None
 
+    def close_async(self):
+        """Release the plan in stream order on the current stream (after the
+        work already queued there), without waiting for the device."""
+        if getattr(self, "_h", None):
+            h, self._h = self._h, None
+            call("bsp_plan_destroy_async", h, _stream())
+
     def __del__(self):
         self.close()
 

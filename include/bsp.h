@@ -182,8 +182,9 @@ typedef struct bsp_plan_info {
 } bsp_plan_info;
 
 /* Build a plan for A (packed LSB-first words[M][ceil(K/32)]).  Runs grouping
- * kernels on `stream`, then synchronises it once to size the plan's device
- * buffers, which the plan owns.  The plan is immutable and may be used from
+ * kernels on `stream` (and, for the tensor-core structures, on a library side
+ * stream joined back into it), synchronising it to size the plan's device
+ * buffers, which the plan owns, and before returning.  The plan is immutable and may be used from
  * any stream afterwards.  params may be NULL (defaults).  The similarity
  * grouping has no counterpart in the reference; its first-fit grouping of
  * disjoint rows is bsp_group_rows.                                           */
@@ -191,6 +192,14 @@ int bsp_plan_create(const uint32_t* words, int64_t M, int64_t K,
                     const bsp_plan_params* params, bsp_plan** plan,
                     bsp_stream_t stream);
 int bsp_plan_destroy(bsp_plan* plan);
+/* Same, without waiting for the device: the plan's device memory goes back
+ * to the library's pool in stream order, after the work already queued on
+ * `stream` (e.g. the SpMM that used the plan).  Work using the plan on other
+ * streams must be ordered before that point by the caller (an event).  The
+ * host object is released at once; the handle is invalid on return.  No
+ * counterpart in the reference, whose device buffers are released with
+ * cudaFree (e.g. source/src/main.cu:1665). */
+int bsp_plan_destroy_async(bsp_plan* plan, bsp_stream_t stream);
 int bsp_plan_get_info(const bsp_plan* plan, bsp_plan_info* info);
 
 /* ======================================================================== */

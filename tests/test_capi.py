@@ -70,6 +70,7 @@ def test_argument_validation_without_gpu():
     assert L.bsp_spmm_i8(fake, 3, 33, 32, fake, 0, 8, 8, fake, 8, fake, 1 << 20, None) == -1
     # plan handles
     assert L.bsp_plan_destroy(None) == 0
+    assert L.bsp_plan_destroy_async(None, None) == 0
     assert L.bsp_plan_get_info(None, None) == -1
     n = C.c_size_t(7)
     assert L.bsp_spmm_workspace(None, 16, C.byref(n)) == 0 and n.value == 0

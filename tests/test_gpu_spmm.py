@@ -230,3 +230,24 @@ def test_proto_bulk_mixed_rows(N, bdt):
     Ci = ops.spmm(wd, 3000, torch.from_numpy(Bi).cuda(), plan=plan).cpu().numpy()
     assert np.array_equal(Ci.astype(np.float64), O.spmm_f64(words, 3000, Bi))
     assert capi.device_status() == 0
+
+
+def test_plan_destroy_async_in_a_loop():
+    """Plans built, used and released in stream order, back to back on one
+    stream without a host wait between steps (the serving-loop pattern):
+    every step's C is exact on integer B."""
+    rng = np.random.default_rng(31)
+    A, _, _ = W.clustered_bits(1024, 2048, n_proto=8, p_proto=0.08, p_flip=0.004, seed_proto=31,
+                               seed_rows=32)
+    words = W.pack_bits(A)
+    wd = words_dev(words)
+    outs = []
+    Bs = [rng.integers(-8, 9, (2048, 256)).astype(np.float32) for _ in range(4)]
+    for Bi in Bs:
+        plan = ops.Plan(wd, 2048, mode=capi.PLAN_PROTO)
+        outs.append(ops.spmm(wd, 2048, torch.from_numpy(Bi).cuda(), plan=plan))
+        plan.close_async()
+    torch.cuda.synchronize()
+    for Bi, C in zip(Bs, outs):
+        assert np.array_equal(C.cpu().numpy().astype(np.float64), O.spmm_f64(words, 2048, Bi))
+    assert capi.device_status() == 0
