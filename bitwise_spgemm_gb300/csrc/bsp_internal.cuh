@@ -53,6 +53,35 @@ template <> __device__ __forceinline__ float from_f32<float>(float x) { return x
 template <> __device__ __forceinline__ __nv_bfloat16 from_f32<__nv_bfloat16>(float x) { return __float2bfloat16_rn(x); }
 template <> __device__ __forceinline__ __half from_f32<__half>(float x) { return __float2half_rn(x); }
 
+// Exclusive scan of one int per thread over the block (≤ 32 warps);
+// smem_warp holds 32 ints; *total = the block's sum.  Ends with a barrier,
+// so smem_warp may be reused right after.
+__device__ __forceinline__ int block_exclusive_scan(int v, int* smem_warp, int* total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(kFull, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) smem_warp[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int s = lane < (int)(blockDim.x >> 5) ? smem_warp[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(kFull, s, o);
+      if (lane >= o) s += y;
+    }
+    smem_warp[lane] = s;  // inclusive warp-sum prefix
+  }
+  __syncthreads();
+  const int before = wid ? smem_warp[wid - 1] : 0;
+  *total = smem_warp[(blockDim.x >> 5) - 1];
+  __syncthreads();
+  return before + x - v;
+}
+
 // Internal launchers (defined in the .cu files, called from capi.cu).
 int launch_pack_rows(const void* dense, int dtype, int64_t M, int64_t K, int64_t ld,
                      uint32_t* words, int msb, cudaStream_t s);

@@ -102,32 +102,6 @@ constexpr int kScanThreads = 256;
 constexpr int kScanItems = 4;
 constexpr int kScanTile = kScanThreads * kScanItems;
 
-__device__ __forceinline__ int block_exclusive_scan(int v, int* smem_warp, int* total) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  int x = v;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int y = __shfl_up_sync(kFull, x, o);
-    if (lane >= o) x += y;
-  }
-  if (lane == 31) smem_warp[wid] = x;
-  __syncthreads();
-  if (wid == 0) {
-    int s = lane < (int)(blockDim.x >> 5) ? smem_warp[lane] : 0;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(kFull, s, o);
-      if (lane >= o) s += y;
-    }
-    smem_warp[lane] = s;  // inclusive warp-sum prefix
-  }
-  __syncthreads();
-  const int before = wid ? smem_warp[wid - 1] : 0;
-  *total = smem_warp[(blockDim.x >> 5) - 1];
-  __syncthreads();
-  return before + x - v;
-}
-
 __global__ void __launch_bounds__(kScanThreads) k_scan_reduce(const int32_t* __restrict__ in, int64_t n,
                                                               int32_t* __restrict__ bsum) {
   __shared__ int sw[32];

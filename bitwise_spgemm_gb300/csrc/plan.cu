@@ -20,7 +20,8 @@
 //  3. buckets with ≥ min_cluster_rows rows become clusters, numbered by an
 //     exclusive scan over "row is a bucket leader" flags (stable: ascending
 //     leader row), so numbering is deterministic;
-//  4. consensus: per-cluster per-column counts (atomicAdd), majority bit;
+//  4. consensus: the rows are listed by cluster, and a CTA per cluster
+//     counts each column's bits (bit-sliced counters) and keeps the majority;
 //  5. every row also looks up, for each pair band (h_2b, h_2b+1), the
 //     cluster whose consensus has the same pair, and keeps the nearest
 //     candidate (Hamming distance, ties → lower cluster id) — this rescues
@@ -97,10 +98,15 @@ __device__ __forceinline__ int nth_set_bit(uint32_t x, int n) {
 // takes bits l, l+32, ... of the group in column order (its source word found
 // by a binary search over the lanes' inclusive bit counts), so every lane
 // hashes about the same number of columns however the bits fall.
+// Then lane 0 inserts the row's band key into the bucket table (open
+// addressing: atomicCAS insert, atomicAdd size, atomicMin leader = lowest
+// row) and records the row's slot (-1: empty row or no key).
 __global__ void __launch_bounds__(256) k_signatures(const uint32_t* __restrict__ words, int64_t M,
                                                     int Kw, int H, uint32_t seed,
                                                     uint32_t* __restrict__ sig,
-                                                    int32_t* __restrict__ nnz) {
+                                                    int32_t* __restrict__ nnz, uint32_t* keys,
+                                                    int32_t* count, int32_t* leader, uint32_t tmask,
+                                                    int32_t* __restrict__ row_slot) {
   const int lane = threadIdx.x & 31;
   const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   if (row >= M) return;
@@ -141,35 +147,90 @@ __global__ void __launch_bounds__(256) k_signatures(const uint32_t* __restrict__
   }
 #pragma unroll
   for (int j = 0; j < kMaxHashes; j++) {
-    if (j >= H) break;
-    const uint32_t m = __reduce_min_sync(kFull, mn[j]);
-    if (lane == j) sig[row * H + j] = m;
+    mn[j] = j < H ? __reduce_min_sync(kFull, mn[j]) : kEmpty;
+    if (j < H && lane == j) sig[row * H + j] = mn[j];
   }
-  if (lane == 0) nnz[row] = cnt;
+  if (lane == 0) {
+    nnz[row] = cnt;
+    const uint32_t key = band_key(mn, H);
+    int32_t found = -1;
+    if (cnt > 0 && key != kEmpty) {
+      uint32_t sl = slot_of(key, tmask);
+      for (uint32_t probe = 0; probe <= tmask; probe++) {
+        const uint32_t prev = atomicCAS(keys + sl, kEmpty, key);
+        if (prev == kEmpty || prev == key) {
+          atomicAdd(count + sl, 1);
+          atomicMin(leader + sl, (int32_t)row);
+          found = (int32_t)sl;
+          break;
+        }
+        sl = (sl + 1) & tmask;
+      }
+    }
+    row_slot[row] = found;
+  }
 }
 
-// Thread per row: insert the row's band key into the bucket table.
-__global__ void k_bucket_insert(const uint32_t* __restrict__ sig, const int32_t* __restrict__ nnz,
-                                int64_t M, int H, uint32_t* keys, int32_t* count, int32_t* leader,
-                                uint32_t tmask, int32_t* __restrict__ row_slot) {
+
+__device__ __forceinline__ int leader_flag(const int32_t* __restrict__ row_slot, const int32_t* __restrict__ count,
+                                           const int32_t* __restrict__ leader, int64_t row, int min_rows) {
+  const int32_t s = row_slot[row];
+  return (s >= 0 && count[s] >= min_rows && leader[s] == (int32_t)row) ? 1 : 0;
+}
+
+// Up to kLeaderScanMax rows, in one CTA (tiles in row order): the leader
+// flags and their exclusive scan (cluster numbers, total in cid[M]), and the
+// exclusive scan of the cluster sizes at leader rows (where each cluster's
+// rows start in the by-cluster row list, total in coff[M]).
+constexpr int kLeaderScanThreads = 1024;
+constexpr int64_t kLeaderScanMax = 32768;
+__global__ void __launch_bounds__(kLeaderScanThreads) k_leader_scan(const int32_t* __restrict__ row_slot,
+                                                                    const int32_t* __restrict__ count,
+                                                                    const int32_t* __restrict__ leader, int64_t M,
+                                                                    int min_rows, int32_t* __restrict__ cid,
+                                                                    int32_t* __restrict__ coff) {
+  __shared__ int sw[32];
+  constexpr int ITEMS = 4, TILE = kLeaderScanThreads * ITEMS;
+  int carry = 0, carry_sz = 0;
+  for (int64_t base = 0; base < M; base += TILE) {
+    int v[ITEMS], z[ITEMS];
+    int sum = 0, sum_sz = 0;
+#pragma unroll
+    for (int j = 0; j < ITEMS; j++) {
+      const int64_t i = base + (int64_t)threadIdx.x * ITEMS + j;
+      v[j] = i < M ? leader_flag(row_slot, count, leader, i, min_rows) : 0;
+      z[j] = v[j] ? count[row_slot[i]] : 0;
+      sum += v[j];
+      sum_sz += z[j];
+    }
+    int total, total_sz;
+    int run = block_exclusive_scan(sum, sw, &total) + carry;
+    int run_sz = block_exclusive_scan(sum_sz, sw, &total_sz) + carry_sz;
+#pragma unroll
+    for (int j = 0; j < ITEMS; j++) {
+      const int64_t i = base + (int64_t)threadIdx.x * ITEMS + j;
+      if (i < M) {
+        cid[i] = run;
+        coff[i] = run_sz;
+      }
+      run += v[j];
+      run_sz += z[j];
+    }
+    carry += total;
+    carry_sz += total_sz;
+  }
+  if (threadIdx.x == 0) {
+    cid[M] = carry;
+    coff[M] = carry_sz;
+  }
+}
+
+__global__ void k_leader_sizes(const int32_t* __restrict__ row_slot, const int32_t* __restrict__ count,
+                               const int32_t* __restrict__ leader, int64_t M, int min_rows,
+                               int32_t* __restrict__ size) {
   const int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (row >= M) return;
-  const uint32_t key = band_key(sig + row * H, H);
-  int32_t found = -1;
-  if (nnz[row] > 0 && key != kEmpty) {
-    uint32_t s = slot_of(key, tmask);
-    for (uint32_t probe = 0; probe <= tmask; probe++) {
-      const uint32_t prev = atomicCAS(keys + s, kEmpty, key);
-      if (prev == kEmpty || prev == key) {
-        atomicAdd(count + s, 1);
-        atomicMin(leader + s, (int32_t)row);
-        found = (int32_t)s;
-        break;
-      }
-      s = (s + 1) & tmask;
-    }
-  }
-  row_slot[row] = found;
+  size[row] = leader_flag(row_slot, count, leader, row, min_rows) ? count[row_slot[row]] : 0;
 }
 
 __global__ void k_leader_flags(const int32_t* __restrict__ row_slot, const int32_t* __restrict__ count,
@@ -177,56 +238,33 @@ __global__ void k_leader_flags(const int32_t* __restrict__ row_slot, const int32
                                int32_t* __restrict__ flag) {
   const int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (row >= M) return;
-  const int32_t s = row_slot[row];
-  flag[row] = (s >= 0 && count[s] >= min_rows && leader[s] == (int32_t)row) ? 1 : 0;
+  flag[row] = leader_flag(row_slot, count, leader, row, min_rows);
 }
 
-__global__ void k_assign(const int32_t* __restrict__ row_slot, const int32_t* __restrict__ count,
-                         const int32_t* __restrict__ leader, const int32_t* __restrict__ cid_of_row,
-                         int64_t M, int min_rows, int32_t* __restrict__ cluster,
-                         int32_t* __restrict__ csize) {
+// Thread per row: the row's cluster (its bucket's number, if the bucket
+// became a cluster) and its place in the by-cluster row list (the order
+// within a cluster follows atomicAdd and does not matter: the list is only
+// counted); the leader row records the cluster's size and list start.
+__global__ void k_cluster_rows(const int32_t* __restrict__ row_slot, const int32_t* __restrict__ count,
+                               const int32_t* __restrict__ leader, const int32_t* __restrict__ cid_of_row,
+                               const int32_t* __restrict__ coff_of_row, int64_t M, int min_rows,
+                               int32_t* __restrict__ cluster, int32_t* __restrict__ csize,
+                               int32_t* __restrict__ cstart, int32_t* cursor, int32_t* __restrict__ rows) {
   const int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (row >= M) return;
-  const int32_t s = row_slot[row];
+  const int32_t sl = row_slot[row];
   int32_t c = -1;
-  if (s >= 0 && count[s] >= min_rows) {
-    c = cid_of_row[leader[s]];
-    if (leader[s] == (int32_t)row) csize[c] = count[s];
+  if (sl >= 0 && count[sl] >= min_rows) {
+    const int32_t L = leader[sl];
+    c = cid_of_row[L];
+    const int32_t base = coff_of_row[L];
+    rows[base + atomicAdd(cursor + c, 1)] = (int32_t)row;
+    if (L == (int32_t)row) {
+      csize[c] = count[sl];
+      cstart[c] = base;
+    }
   }
   cluster[row] = c;
-}
-
-// Thread per (row, word) of clustered rows: per-column bit counts.
-__global__ void k_count_bits(const uint32_t* __restrict__ words, int64_t M, int Kw, int64_t K,
-                             const int32_t* __restrict__ cluster, int32_t* __restrict__ counts) {
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= M * Kw) return;
-  const int64_t row = t / Kw;
-  const int w = (int)(t - row * Kw);
-  const int32_t c = cluster[row];
-  if (c < 0) return;
-  uint32_t x = words[t];
-  while (x) {
-    const int b = __ffs(x) - 1;
-    x &= x - 1;
-    atomicAdd(counts + (int64_t)c * K + w * 32 + b, 1);
-  }
-}
-
-// Thread per (cluster, word): majority vote.
-__global__ void k_majority(const int32_t* __restrict__ counts, const int32_t* __restrict__ csize,
-                           int64_t n_clusters, int Kw, int64_t K, uint32_t* __restrict__ cons) {
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= n_clusters * Kw) return;
-  const int64_t c = t / Kw;
-  const int w = (int)(t - c * Kw);
-  const int32_t sz = csize[c];
-  uint32_t m = 0;
-  for (int b = 0; b < 32; b++) {
-    const int64_t k = (int64_t)w * 32 + b;
-    if (k < K && 2 * counts[c * K + k] > sz) m |= 1u << b;
-  }
-  cons[t] = m;
 }
 
 __device__ __forceinline__ uint32_t pair_key(uint32_t a, uint32_t b) {
@@ -238,26 +276,121 @@ __device__ __forceinline__ uint32_t pair_key(uint32_t a, uint32_t b) {
   return k == kEmpty ? kEmpty - 1 : k;
 }
 
-// Tables j = 0..H/2-1: pair band (h_2j, h_2j+1) of consensus c → lowest c.
-__global__ void k_alt_insert(const uint32_t* __restrict__ csig, int64_t n_clusters, int H,
-                             uint32_t* keys, int32_t* vals, uint32_t tmask) {
-  const int NB = H / 2;
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= n_clusters * NB) return;
-  const int64_t c = t / NB;
-  const int j = (int)(t - c * NB);
-  const uint32_t key = pair_key(csig[c * H + 2 * j], csig[c * H + 2 * j + 1]);
-  if (key == kEmpty) return;
-  uint32_t* K = keys + (int64_t)j * (tmask + 1);
-  int32_t* V = vals + (int64_t)j * (tmask + 1);
-  uint32_t s = slot_of(key, tmask);
-  for (uint32_t probe = 0; probe <= tmask; probe++) {
-    const uint32_t prev = atomicCAS(K + s, kEmpty, key);
-    if (prev == kEmpty || prev == key) {
-      atomicMin(V + s, (int32_t)c);
-      return;
+// Block per cluster: the consensus words (majority of the cluster's rows per
+// column), their popcount (stats[4]) and MinHash values (as k_signatures
+// computes them for a row), and the consensus's pair bands (h_2j, h_2j+1)
+// inserted into tables j = 0..H/2-1 (key → lowest cluster id).  Thread w
+// counts column bits of word w over the cluster's rows with 32 bit-sliced
+// counters (plane p holds bit p of the 32 columns' counts; adding a row's
+// word is a ripple-carry over the planes), then compares every count with
+// floor(size/2) in the same bit-sliced form: 2·count > size.
+constexpr int kConsThreads = 256;
+constexpr int kConsRowChunk = 1024;  // row indices staged in shared memory at a time
+constexpr int kConsInFlight = 16;    // word loads in flight per thread
+__global__ void __launch_bounds__(kConsThreads) k_consensus(const uint32_t* __restrict__ words, int Kw,
+                                                            const int32_t* __restrict__ rows,
+                                                            const int32_t* __restrict__ cstart,
+                                                            const int32_t* __restrict__ csize,
+                                                            int H, uint32_t seed, uint32_t* __restrict__ cons,
+                                                            uint32_t* akeys, int32_t* avals, uint32_t tmask,
+                                                            unsigned long long* stats) {
+  __shared__ uint32_t wmin[kMaxHashes][kConsThreads / 32];
+  __shared__ unsigned wpop[kConsThreads / 32];
+  const int64_t c = blockIdx.x;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int32_t sz = csize[c];
+  const int32_t* crow = rows + cstart[c];
+  const uint32_t half = (uint32_t)sz >> 1;
+  uint32_t mn[kMaxHashes];
+#pragma unroll
+  for (int j = 0; j < kMaxHashes; j++) mn[j] = kEmpty;
+  unsigned pop = 0;
+  __shared__ int32_t srow[kConsRowChunk];
+  for (int wb = 0; wb < Kw; wb += kConsThreads) {  // uniform: every thread runs the same chunks
+    const int w = wb + (int)threadIdx.x;
+    const bool wv = w < Kw;
+    uint32_t plane[32];
+#pragma unroll
+    for (int p = 0; p < 32; p++) plane[p] = 0u;
+    for (int r0 = 0; r0 < sz; r0 += kConsRowChunk) {
+      const int nr = min(kConsRowChunk, sz - r0);
+      __syncthreads();
+      for (int i = threadIdx.x; i < nr; i += kConsThreads) srow[i] = crow[r0 + i];
+      __syncthreads();
+      for (int i0 = 0; i0 < nr; i0 += kConsInFlight) {
+        uint32_t xs[kConsInFlight];
+#pragma unroll
+        for (int u = 0; u < kConsInFlight; u++)
+          xs[u] = (wv && i0 + u < nr) ? __ldg(words + (int64_t)srow[i0 + u] * Kw + w) : 0u;
+#pragma unroll
+        for (int u = 0; u < kConsInFlight; u++) {
+          uint32_t x = xs[u];
+#pragma unroll
+          for (int p = 0; p < 32; p++) {
+            const uint32_t carry = plane[p] & x;
+            plane[p] ^= x;
+            x = carry;
+            if (!x) break;
+          }
+        }
+      }
     }
-    s = (s + 1) & tmask;
+    uint32_t gt = 0u, eq = ~0u;  // count > half, count == half (so far, high planes first)
+#pragma unroll
+    for (int p = 31; p >= 0; p--) {
+      if ((half >> p) & 1u) {
+        eq &= plane[p];
+      } else {
+        gt |= eq & plane[p];
+        eq &= ~plane[p];
+      }
+    }
+    if (!wv) continue;
+    uint32_t m = gt;
+    cons[c * Kw + w] = m;
+    pop += __popc(m);
+    while (m) {
+      const int b = __ffs(m) - 1;
+      m &= m - 1;
+      const uint32_t k = (uint32_t)(w * 32 + b);
+#pragma unroll
+      for (int j = 0; j < kMaxHashes; j++)
+        if (j < H) mn[j] = min(mn[j], mix32(k, (uint32_t)j, seed));
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < kMaxHashes; j++) {
+    const uint32_t v = __reduce_min_sync(kFull, mn[j]);
+    if (lane == 0) wmin[j][wid] = v;
+  }
+  pop = __reduce_add_sync(kFull, pop);
+  if (lane == 0) wpop[wid] = pop;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long total = 0;
+    for (int i = 0; i < kConsThreads / 32; i++) total += wpop[i];
+    if (total) atomicAdd(stats + 4, total);
+  }
+  const int j = threadIdx.x;
+  if (j < H / 2) {
+    uint32_t a = kEmpty, b = kEmpty;
+    for (int i = 0; i < kConsThreads / 32; i++) {
+      a = min(a, wmin[2 * j][i]);
+      b = min(b, wmin[2 * j + 1][i]);
+    }
+    const uint32_t key = pair_key(a, b);
+    if (key == kEmpty) return;
+    uint32_t* Kt = akeys + (int64_t)j * (tmask + 1);
+    int32_t* Vt = avals + (int64_t)j * (tmask + 1);
+    uint32_t sl = slot_of(key, tmask);
+    for (uint32_t probe = 0; probe <= tmask; probe++) {
+      const uint32_t prev = atomicCAS(Kt + sl, kEmpty, key);
+      if (prev == kEmpty || prev == key) {
+        atomicMin(Vt + sl, (int32_t)c);
+        return;
+      }
+      sl = (sl + 1) & tmask;
+    }
   }
 }
 
@@ -324,12 +457,6 @@ __global__ void __launch_bounds__(256) k_finalize_rows(
   }
 }
 
-__global__ void k_cons_popc(const uint32_t* __restrict__ cons, int64_t n, unsigned long long* stats) {
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int c = t < n ? __popc(cons[t]) : 0;
-  const unsigned s = __reduce_add_sync(kFull, (unsigned)c);
-  if ((threadIdx.x & 31) == 0 && s) atomicAdd(stats + 4, (unsigned long long)s);
-}
 
 // Warp per clustered row: delta entries in ascending column order.
 __global__ void __launch_bounds__(256) k_delta_fill(const uint32_t* __restrict__ words, int64_t M,
@@ -518,6 +645,7 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
   const size_t o_slot = take(sizeof(int32_t) * M);
   const size_t o_flag = take(sizeof(int32_t) * M);
   const size_t o_cid = take(sizeof(int32_t) * (M + 1));
+  const size_t o_coff = take(sizeof(int32_t) * (M + 1));
   const size_t o_scan = take(scan_workspace_bytes(M + 1));
   const size_t o_stats = take(sizeof(unsigned long long) * 8);
   const size_t o_dcnt = take(sizeof(int32_t) * M);
@@ -532,6 +660,7 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
   int32_t* slot = (int32_t*)(T + o_slot);
   int32_t* flag = (int32_t*)(T + o_flag);
   int32_t* cid = (int32_t*)(T + o_cid);
+  int32_t* coff = (int32_t*)(T + o_coff);
   void* scanws = T + o_scan;
   unsigned long long* stats = (unsigned long long*)(T + o_stats);
   int32_t* dcnt = (int32_t*)(T + o_dcnt);
@@ -564,19 +693,23 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
 
   const unsigned wgrid = (unsigned)ceil_div(M, 8);    // warp-per-row kernels, 256 threads
   const unsigned tgrid = (unsigned)ceil_div(M, 256);  // thread-per-row kernels
-  k_signatures<<<wgrid, 256, 0, s>>>(words, M, Kw, H, prm->seed, sig, nnz);
-  k_bucket_insert<<<tgrid, 256, 0, s>>>(sig, nnz, M, H, keys, cnt, lead, tsize - 1, slot);
-  k_leader_flags<<<tgrid, 256, 0, s>>>(slot, cnt, lead, M, min_rows, flag);
+  k_signatures<<<wgrid, 256, 0, s>>>(words, M, Kw, H, prm->seed, sig, nnz, keys, cnt, lead, tsize - 1, slot);
+  if (M <= kLeaderScanMax) {
+    k_leader_scan<<<1, kLeaderScanThreads, 0, s>>>(slot, cnt, lead, M, min_rows, cid, coff);
+  } else {
+    k_leader_flags<<<tgrid, 256, 0, s>>>(slot, cnt, lead, M, min_rows, flag);
+    BSP_LAUNCHED();
+    BSP_TRY(launch_scan_i32(flag, M, cid, scanws, s));
+    k_leader_sizes<<<tgrid, 256, 0, s>>>(slot, cnt, lead, M, min_rows, flag);
+    BSP_LAUNCHED();
+    BSP_TRY(launch_scan_i32(flag, M, coff, scanws, s));
+  }
   BSP_LAUNCHED();
-  BSP_TRY(launch_scan_i32(flag, M, cid, scanws, s));
   int32_t n_clusters = 0;
   BSP_CUDA(cudaMemcpyAsync(&n_clusters, cid + M, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
   BSP_CUDA(cudaStreamSynchronize(s));
 
-  // Per-column counts need n_clusters*K ints; beyond 1 GiB the plan stays direct.
-  const bool can_cluster = n_clusters > 0 &&
-                           (double)n_clusters * (double)K * 4.0 <= (double)(1ull << 30) &&
-                           prm->mode != BSP_PLAN_DIRECT;
+  const bool can_cluster = n_clusters > 0 && prm->mode != BSP_PLAN_DIRECT;
   const int64_t ncl = can_cluster ? n_clusters : 0;
 
   // ---- plan storage (cluster map, delta pointers, consensus) -------------
@@ -600,37 +733,30 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
     const uint32_t asize = pow2_at_least(2 * ncl);
     size_t off2 = 0;
     auto take2 = [&](size_t bytes) { const size_t o = off2; off2 += al256(bytes); return o; };
-    const size_t q_counts = take2(sizeof(int32_t) * ncl * K);
     const size_t q_csize = take2(sizeof(int32_t) * ncl);
-    const size_t q_csig = take2(sizeof(uint32_t) * ncl * H);
-    const size_t q_cnnz = take2(sizeof(int32_t) * ncl);
+    const size_t q_cstart = take2(sizeof(int32_t) * ncl);
+    const size_t q_cursor = take2(sizeof(int32_t) * ncl);
+    const size_t q_rows = take2(sizeof(int32_t) * M);
     const size_t q_akeys = take2(sizeof(uint32_t) * asize * H);
     const size_t q_avals = take2(sizeof(int32_t) * asize * H);
     DevBuf t2;
     BSP_TRY(t2.alloc(off2, s));
     char* T2 = static_cast<char*>(t2.p);
-    int32_t* counts = (int32_t*)(T2 + q_counts);
     int32_t* csize = (int32_t*)(T2 + q_csize);
-    uint32_t* csig = (uint32_t*)(T2 + q_csig);
-    int32_t* cnnz = (int32_t*)(T2 + q_cnnz);
+    int32_t* cstart = (int32_t*)(T2 + q_cstart);
+    int32_t* cursor = (int32_t*)(T2 + q_cursor);
+    int32_t* crows = (int32_t*)(T2 + q_rows);
     uint32_t* akeys = (uint32_t*)(T2 + q_akeys);
     int32_t* avals = (int32_t*)(T2 + q_avals);
-    BSP_CUDA(cudaMemsetAsync(counts, 0, sizeof(int32_t) * ncl * K, s));
+    BSP_CUDA(cudaMemsetAsync(cursor, 0, sizeof(int32_t) * ncl, s));
     BSP_CUDA(cudaMemsetAsync(akeys, 0xff, sizeof(uint32_t) * asize * H, s));
     BSP_CUDA(cudaMemsetAsync(avals, 0x7f, sizeof(int32_t) * asize * H, s));
-    k_assign<<<tgrid, 256, 0, s>>>(slot, cnt, lead, cid, M, min_rows, plan->row_cluster, csize);
-    k_count_bits<<<(unsigned)ceil_div(M * Kw, 256), 256, 0, s>>>(words, M, Kw, K, plan->row_cluster,
-                                                                 counts);
-    k_majority<<<(unsigned)ceil_div(ncl * Kw, 256), 256, 0, s>>>(counts, csize, ncl, Kw, K,
-                                                                 plan->cons);
-    k_signatures<<<(unsigned)ceil_div(ncl, 8), 256, 0, s>>>(plan->cons, ncl, Kw, H, prm->seed,
-                                                            csig, cnnz);
-    if (H >= 2)
-      k_alt_insert<<<(unsigned)ceil_div(ncl * (H / 2), 256), 256, 0, s>>>(csig, ncl, H, akeys,
-                                                                        avals, asize - 1);
+    k_cluster_rows<<<tgrid, 256, 0, s>>>(slot, cnt, lead, cid, coff, M, min_rows, plan->row_cluster, csize, cstart,
+                                         cursor, crows);
+    k_consensus<<<(unsigned)ncl, kConsThreads, 0, s>>>(words, Kw, crows, cstart, csize, H, prm->seed, plan->cons,
+                                                      akeys, avals, asize - 1, stats);
     k_finalize_rows<<<wgrid, 256, 0, s>>>(words, M, Kw, H, sig, nnz, plan->cons, ncl, akeys, avals,
                                           asize - 1, plan->row_cluster, dcnt, stats);
-    k_cons_popc<<<(unsigned)ceil_div(ncl * Kw, 256), 256, 0, s>>>(plan->cons, ncl * Kw, stats);
     BSP_LAUNCHED();
   } else {
     BSP_CUDA(cudaMemsetAsync(plan->row_cluster, 0xff, sizeof(int32_t) * M, s));
