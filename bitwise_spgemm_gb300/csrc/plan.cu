@@ -33,10 +33,12 @@
 // deterministic function of A.  The tensor-core structures (occupancy bitmaps,
 // A's words by column) depend on A alone and are built on a side stream
 // meanwhile.
+#include <algorithm>
 #include <climits>
 #include <mutex>
 #include <cstdlib>
 #include <new>
+#include <vector>
 
 #include "bsp_internal.cuh"
 #include "plan.cuh"
@@ -48,7 +50,7 @@ namespace {
 constexpr uint32_t kEmpty = 0xffffffffu;
 constexpr int kMaxHashes = 8;
 
-__device__ __forceinline__ uint32_t mix32(uint32_t k, uint32_t j, uint32_t seed) {
+__host__ __device__ __forceinline__ uint32_t mix32(uint32_t k, uint32_t j, uint32_t seed) {
   // murmur3 finaliser of a per-function offset key
   uint32_t h = k * 0x9e3779b1u + (j + 1u) * 0x85ebca77u + seed;
   h ^= h >> 16;
@@ -93,16 +95,27 @@ __device__ __forceinline__ int nth_set_bit(uint32_t x, int n) {
   return pos;
 }
 
-// Warp per row: H MinHash values and the popcount.  The row's words are taken
-// 32 at a time (one per lane) and their set bits are dealt out evenly: lane l
-// takes bits l, l+32, ... of the group in column order (its source word found
-// by a binary search over the lanes' inclusive bit counts), so every lane
-// hashes about the same number of columns however the bits fall.
+// Warp per row: H MinHash values and the popcount.
+//
+// With `perm` (perm[j*K + t] = the column with the t-th smallest mix(., j);
+// mix is a bijection of the column for fixed j, so the order is strict), the
+// minimum over the row's columns of mix(k, j) is mix of the first column in
+// that order that the row holds: lanes test 32 positions of the order at a
+// time against the row's words and a ballot finds the first hit.  A row of
+// density d needs about 1/d probes per function instead of hashing every
+// set bit H times.  Rows sparser than 1/64, and functions without a hit in
+// kPermRounds rounds, take the direct path: the row's words 32 at a time
+// (one per lane), their set bits dealt out evenly — lane l takes bits l,
+// l+32, ... of the group in column order, its source word found by a binary
+// search over the lanes' inclusive bit counts — and hashed.  Both give the
+// same minimum.
 // Then lane 0 inserts the row's band key into the bucket table (open
 // addressing: atomicCAS insert, atomicAdd size, atomicMin leader = lowest
 // row) and records the row's slot (-1: empty row or no key).
+constexpr int kPermRounds = 8;
 __global__ void __launch_bounds__(256) k_signatures(const uint32_t* __restrict__ words, int64_t M,
-                                                    int Kw, int H, uint32_t seed,
+                                                    int Kw, int64_t K, int H, uint32_t seed,
+                                                    const uint32_t* __restrict__ perm,
                                                     uint32_t* __restrict__ sig,
                                                     int32_t* __restrict__ nnz, uint32_t* keys,
                                                     int32_t* count, int32_t* leader, uint32_t tmask,
@@ -113,8 +126,35 @@ __global__ void __launch_bounds__(256) k_signatures(const uint32_t* __restrict__
   uint32_t mn[kMaxHashes];
 #pragma unroll
   for (int j = 0; j < kMaxHashes; j++) mn[j] = kEmpty;
-  int cnt = 0;
   const uint32_t* r = words + row * Kw;
+  int cnt = 0;
+  for (int w = lane; w < Kw; w += 32) cnt += __popc(__ldg(r + w));
+  cnt = (int)__reduce_add_sync(kFull, (unsigned)cnt);
+  uint32_t miss = (1u << H) - 1u;  // functions still to compute directly
+  if (perm && (int64_t)cnt * 64 >= K) {
+#pragma unroll
+    for (int j = 0; j < kMaxHashes; j++) {
+      if (j >= H) break;
+      const uint32_t* pj = perm + (int64_t)j * K;
+      for (int rd = 0; rd < kPermRounds; rd++) {
+        const int64_t t = (int64_t)rd * 32 + lane;
+        uint32_t k = 0u;
+        bool hit = false;
+        if (t < K) {
+          k = __ldg(pj + t);
+          hit = (__ldg(r + (k >> 5)) >> (k & 31)) & 1u;
+        }
+        const uint32_t b = __ballot_sync(kFull, hit);
+        if (b) {
+          mn[j] = mix32(__shfl_sync(kFull, k, __ffs(b) - 1), (uint32_t)j, seed);
+          miss &= ~(1u << j);
+          break;
+        }
+        if ((int64_t)(rd + 1) * 32 >= K) break;
+      }
+    }
+  }
+  if (miss) {
   for (int g = 0; g < Kw; g += 32) {
     const uint32_t x = (g + lane < Kw) ? __ldg(r + g + lane) : 0u;
     const int c = __popc(x);
@@ -126,7 +166,6 @@ __global__ void __launch_bounds__(256) k_signatures(const uint32_t* __restrict__
     }
     const int excl = incl - c;
     const int total = __shfl_sync(kFull, incl, 31);
-    cnt += total;
     for (int b0 = 0; b0 < total; b0 += 32) {
       const int gi = b0 + lane;  // this lane's bit of the group, in column order
       int src = 0;               // lanes whose words end before bit gi
@@ -141,9 +180,10 @@ __global__ void __launch_bounds__(256) k_signatures(const uint32_t* __restrict__
         const uint32_t k = (uint32_t)((g + src) * 32 + nth_set_bit(wx, gi - ex));
 #pragma unroll
         for (int j = 0; j < kMaxHashes; j++)
-          if (j < H) mn[j] = min(mn[j], mix32(k, (uint32_t)j, seed));
+          if ((miss >> j) & 1u) mn[j] = min(mn[j], mix32(k, (uint32_t)j, seed));
       }
     }
+  }
   }
 #pragma unroll
   for (int j = 0; j < kMaxHashes; j++) {
@@ -589,6 +629,51 @@ cudaStream_t side_stream() {
   return streams[dev];
 }
 
+// Column orders of the MinHash functions (perm of k_signatures) per device
+// and (K, H, seed): sorted on the host at first use, kept until exit (at most
+// 16 orders, K ≤ kPermMaxK; otherwise the signatures are computed directly).
+constexpr int64_t kPermMaxK = (int64_t)1 << 18;
+const uint32_t* minhash_order(int64_t K, int H, uint32_t seed) {
+  struct Entry {
+    int dev;
+    int64_t K;
+    int H;
+    uint32_t seed;
+    uint32_t* d;
+  };
+  static std::mutex mu;
+  static std::vector<Entry> cache;
+  if (K < 1 || K > kPermMaxK || H < 1 || H > kMaxHashes) return nullptr;
+  const char* e = getenv("BSP_MINHASH_DIRECT");  // comparisons: hash every set bit
+  if (e && e[0] == '1') return nullptr;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+  std::lock_guard<std::mutex> lk(mu);
+  for (const Entry& e : cache)
+    if (e.dev == dev && e.K == K && e.H == H && e.seed == seed) return e.d;
+  if (cache.size() >= 16) return nullptr;
+  std::vector<uint64_t> key((size_t)K);
+  std::vector<uint32_t> host((size_t)H * (size_t)K);
+  for (int j = 0; j < H; j++) {
+    for (int64_t k = 0; k < K; k++) key[k] = ((uint64_t)mix32((uint32_t)k, (uint32_t)j, seed) << 32) | (uint64_t)k;
+    std::sort(key.begin(), key.end());
+    for (int64_t t = 0; t < K; t++) host[(size_t)j * K + t] = (uint32_t)key[t];
+  }
+  uint32_t* d = nullptr;
+  const size_t bytes = host.size() * sizeof(uint32_t);
+  if (cudaMalloc(&d, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (cudaMemcpy(d, host.data(), bytes, cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(d);
+    return nullptr;
+  }
+  cache.push_back(Entry{dev, K, H, seed, d});
+  return d;
+}
+
 // Work forked from stream `s` onto the side stream: join() makes `s` wait for
 // it; the destructor joins too (and frees the events), so temporaries that
 // are freed on `s` afterwards outlive the side work on every return path.
@@ -693,7 +778,8 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
 
   const unsigned wgrid = (unsigned)ceil_div(M, 8);    // warp-per-row kernels, 256 threads
   const unsigned tgrid = (unsigned)ceil_div(M, 256);  // thread-per-row kernels
-  k_signatures<<<wgrid, 256, 0, s>>>(words, M, Kw, H, prm->seed, sig, nnz, keys, cnt, lead, tsize - 1, slot);
+  k_signatures<<<wgrid, 256, 0, s>>>(words, M, Kw, K, H, prm->seed, minhash_order(K, H, prm->seed), sig, nnz, keys,
+                                     cnt, lead, tsize - 1, slot);
   if (M <= kLeaderScanMax) {
     k_leader_scan<<<1, kLeaderScanThreads, 0, s>>>(slot, cnt, lead, M, min_rows, cid, coff);
   } else {

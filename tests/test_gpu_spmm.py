@@ -251,3 +251,43 @@ def test_plan_destroy_async_in_a_loop():
     for Bi, C in zip(Bs, outs):
         assert np.array_equal(C.cpu().numpy().astype(np.float64), O.spmm_f64(words, 2048, Bi))
     assert capi.device_status() == 0
+
+
+_PATHS_SCRIPT = r"""
+import json, sys, hashlib
+import numpy as np, torch
+sys.path.insert(0, sys.argv[1])
+sys.path.insert(0, sys.argv[1] + "/tests")
+from bitwise_spgemm_gb300 import capi, ops
+from bitwise_spgemm_gb300 import workloads as W
+from gpu_util import words_dev
+rng = np.random.default_rng(41)
+A, _, _ = W.clustered_bits(2048, 3000, n_proto=12, p_proto=0.08, p_flip=0.003, seed_proto=41, seed_rows=42)
+A[::7] = rng.random((A[::7].shape[0], 3000)) < 0.004   # sparser than 1/64: direct hashing
+A[3::11] = rng.random((A[3::11].shape[0], 3000)) < 0.5  # dense rows
+wd = words_dev(W.pack_bits(A))
+plan = ops.Plan(wd, 3000)
+Bi = torch.from_numpy(rng.integers(-8, 9, (3000, 64)).astype(np.float32)).cuda()
+C = ops.spmm(wd, 3000, Bi, plan=plan).cpu().numpy()
+print(json.dumps({"info": plan.info(), "C": hashlib.sha1(C.tobytes()).hexdigest()}))
+"""
+
+
+def test_minhash_paths_agree():
+    """The signature kernel's column-order scan and its direct hashing of
+    every set bit give the same MinHash values, hence the same plan (same
+    prototypes and delta lists) and the same C, bit for bit."""
+    import json
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    outs = []
+    for direct in ("0", "1"):
+        env = dict(os.environ, BSP_MINHASH_DIRECT=direct)
+        r = subprocess.run([sys.executable, "-c", _PATHS_SCRIPT, root], env=env, capture_output=True,
+                           text=True, timeout=300)
+        assert r.returncode == 0, r.stderr[-2000:]
+        outs.append(json.loads(r.stdout.strip().splitlines()[-1]))
+    assert outs[0] == outs[1]
+    assert outs[0]["info"]["mode"] == capi.PLAN_PROTO
