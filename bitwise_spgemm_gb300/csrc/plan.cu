@@ -674,6 +674,61 @@ const uint32_t* minhash_order(int64_t K, int H, uint32_t seed) {
   return d;
 }
 
+// Timing-free events for plan builds, reused across builds (per device).
+std::mutex g_event_mu;
+std::vector<cudaEvent_t> g_events[64];
+int event_acquire(cudaEvent_t* e) {
+  int dev = 0;
+  BSP_CUDA(cudaGetDevice(&dev));
+  if (dev >= 0 && dev < 64) {
+    std::lock_guard<std::mutex> lk(g_event_mu);
+    if (!g_events[dev].empty()) {
+      *e = g_events[dev].back();
+      g_events[dev].pop_back();
+      return BSP_OK;
+    }
+  }
+  BSP_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+  return BSP_OK;
+}
+void event_release(cudaEvent_t e) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64) {
+    std::lock_guard<std::mutex> lk(g_event_mu);
+    if (g_events[dev].size() < 64) {
+      g_events[dev].push_back(e);
+      return;
+    }
+  }
+  cudaEventDestroy(e);
+}
+
+// Up to four arrays of 32-bit words filled with a value each, in one launch.
+struct Fill {
+  uint32_t* p;
+  int64_t n;
+  uint32_t v;
+};
+__global__ void k_fill4(Fill a, Fill b, Fill c, Fill d) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;; i += stride) {
+    bool any = false;
+    if (i < a.n) { a.p[i] = a.v; any = true; }
+    if (i < b.n) { b.p[i] = b.v; any = true; }
+    if (i < c.n) { c.p[i] = c.v; any = true; }
+    if (i < d.n) { d.p[i] = d.v; any = true; }
+    if (!any) break;
+  }
+}
+int launch_fill4(Fill a, Fill b, Fill c, Fill d, cudaStream_t s) {
+  const int64_t n = std::max(std::max(a.n, b.n), std::max(c.n, d.n));
+  if (n <= 0) return BSP_OK;
+  const int64_t blocks = std::min<int64_t>(ceil_div(n, 256), (int64_t)num_sms() * 8);
+  k_fill4<<<(unsigned)blocks, 256, 0, s>>>(a, b, c, d);
+  BSP_LAUNCHED();
+  return BSP_OK;
+}
+
 // Work forked from stream `s` onto the side stream: join() makes `s` wait for
 // it; the destructor joins too (and frees the events), so temporaries that
 // are freed on `s` afterwards outlive the side work on every return path.
@@ -685,8 +740,8 @@ struct SideFork {
     s = main;
     side = side_stream();
     if (!side) return BSP_OK;  // no side stream: the work runs on `s`
-    BSP_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
-    BSP_CUDA(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
+    BSP_TRY(event_acquire(&fork));
+    BSP_TRY(event_acquire(&done));
     BSP_CUDA(cudaEventRecord(fork, s));
     BSP_CUDA(cudaStreamWaitEvent(side, fork, 0));
     joined = false;
@@ -702,8 +757,8 @@ struct SideFork {
   }
   ~SideFork() {
     join();
-    if (fork) cudaEventDestroy(fork);
-    if (done) cudaEventDestroy(done);
+    if (fork) event_release(fork);
+    if (done) event_release(done);
   }
 };
 
@@ -750,10 +805,8 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
   unsigned long long* stats = (unsigned long long*)(T + o_stats);
   int32_t* dcnt = (int32_t*)(T + o_dcnt);
 
-  BSP_CUDA(cudaMemsetAsync(keys, 0xff, sizeof(uint32_t) * tsize, s));
-  BSP_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * tsize, s));
-  BSP_CUDA(cudaMemsetAsync(lead, 0x7f, sizeof(int32_t) * tsize, s));
-  BSP_CUDA(cudaMemsetAsync(stats, 0, sizeof(unsigned long long) * 8, s));
+  BSP_TRY(launch_fill4(Fill{keys, tsize, kEmpty}, Fill{(uint32_t*)cnt, tsize, 0u},
+                       Fill{(uint32_t*)lead, tsize, 0x7f7f7f7fu}, Fill{(uint32_t*)stats, 16, 0u}, s));
 
   // ---- tensor-core structures: occupancy bitmaps and A's words by column
   // (the producers then load the words of 32 consecutive rows or columns as
@@ -834,9 +887,8 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
     int32_t* crows = (int32_t*)(T2 + q_rows);
     uint32_t* akeys = (uint32_t*)(T2 + q_akeys);
     int32_t* avals = (int32_t*)(T2 + q_avals);
-    BSP_CUDA(cudaMemsetAsync(cursor, 0, sizeof(int32_t) * ncl, s));
-    BSP_CUDA(cudaMemsetAsync(akeys, 0xff, sizeof(uint32_t) * asize * H, s));
-    BSP_CUDA(cudaMemsetAsync(avals, 0x7f, sizeof(int32_t) * asize * H, s));
+    BSP_TRY(launch_fill4(Fill{(uint32_t*)cursor, ncl, 0u}, Fill{akeys, (int64_t)asize * H, kEmpty},
+                         Fill{(uint32_t*)avals, (int64_t)asize * H, 0x7f7f7f7fu}, Fill{nullptr, 0, 0u}, s));
     k_cluster_rows<<<tgrid, 256, 0, s>>>(slot, cnt, lead, cid, coff, M, min_rows, plan->row_cluster, csize, cstart,
                                          cursor, crows);
     k_consensus<<<(unsigned)ncl, kConsThreads, 0, s>>>(words, Kw, crows, cstart, csize, H, prm->seed, plan->cons,
