@@ -319,14 +319,18 @@ __device__ __forceinline__ uint32_t pair_key(uint32_t a, uint32_t b) {
 // Block per cluster: the consensus words (majority of the cluster's rows per
 // column), their popcount (stats[4]) and MinHash values (as k_signatures
 // computes them for a row), and the consensus's pair bands (h_2j, h_2j+1)
-// inserted into tables j = 0..H/2-1 (key → lowest cluster id).  Thread w
-// counts column bits of word w over the cluster's rows with 32 bit-sliced
-// counters (plane p holds bit p of the 32 columns' counts; adding a row's
-// word is a ripple-carry over the planes), then compares every count with
-// floor(size/2) in the same bit-sliced form: 2·count > size.
-constexpr int kConsThreads = 256;
+// inserted into tables j = 0..H/2-1 (key → lowest cluster id).  For each
+// block of 256 words, thread (g, w) counts word w's bits over rows g, g+4,
+// ... of the cluster with bit-sliced counters (plane p holds bit p of the 32
+// columns' counts; adding a row's word is a ripple carry over the planes),
+// turns them into per-column counts and adds those into shared memory; then
+// the group-0 thread of word w keeps the columns with 2·count > size.
+constexpr int kConsWords = 256;
+constexpr int kConsGroups = 4;
+constexpr int kConsThreads = kConsWords * kConsGroups;
 constexpr int kConsRowChunk = 1024;  // row indices staged in shared memory at a time
-constexpr int kConsInFlight = 16;    // word loads in flight per thread
+constexpr int kConsInFlight = 8;     // word loads in flight per thread
+constexpr int kConsPlanes = 9;       // a group counts ≤ kConsRowChunk / kConsGroups = 256 rows per chunk
 __global__ void __launch_bounds__(kConsThreads) k_consensus(const uint32_t* __restrict__ words, int Kw,
                                                             const int32_t* __restrict__ rows,
                                                             const int32_t* __restrict__ cstart,
@@ -334,39 +338,44 @@ __global__ void __launch_bounds__(kConsThreads) k_consensus(const uint32_t* __re
                                                             int H, uint32_t seed, uint32_t* __restrict__ cons,
                                                             uint32_t* akeys, int32_t* avals, uint32_t tmask,
                                                             unsigned long long* stats) {
+  static_assert(kConsRowChunk / kConsGroups < (1 << kConsPlanes), "planes");
   __shared__ uint32_t wmin[kMaxHashes][kConsThreads / 32];
   __shared__ unsigned wpop[kConsThreads / 32];
+  __shared__ int32_t srow[kConsRowChunk];
+  __shared__ int32_t colcnt[32 * kConsWords];  // [bit][word]
   const int64_t c = blockIdx.x;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int g = threadIdx.x / kConsWords, wl = threadIdx.x % kConsWords;
   const int32_t sz = csize[c];
   const int32_t* crow = rows + cstart[c];
-  const uint32_t half = (uint32_t)sz >> 1;
   uint32_t mn[kMaxHashes];
 #pragma unroll
   for (int j = 0; j < kMaxHashes; j++) mn[j] = kEmpty;
   unsigned pop = 0;
-  __shared__ int32_t srow[kConsRowChunk];
-  for (int wb = 0; wb < Kw; wb += kConsThreads) {  // uniform: every thread runs the same chunks
-    const int w = wb + (int)threadIdx.x;
+  for (int wb = 0; wb < Kw; wb += kConsWords) {  // uniform: every thread runs the same blocks and chunks
+    const int w = wb + wl;
     const bool wv = w < Kw;
-    uint32_t plane[32];
-#pragma unroll
-    for (int p = 0; p < 32; p++) plane[p] = 0u;
+    for (int i = threadIdx.x; i < 32 * kConsWords; i += kConsThreads) colcnt[i] = 0;
     for (int r0 = 0; r0 < sz; r0 += kConsRowChunk) {
       const int nr = min(kConsRowChunk, sz - r0);
       __syncthreads();
       for (int i = threadIdx.x; i < nr; i += kConsThreads) srow[i] = crow[r0 + i];
       __syncthreads();
-      for (int i0 = 0; i0 < nr; i0 += kConsInFlight) {
+      uint32_t plane[kConsPlanes];
+#pragma unroll
+      for (int p = 0; p < kConsPlanes; p++) plane[p] = 0u;
+      for (int i0 = g; i0 < nr; i0 += kConsGroups * kConsInFlight) {
         uint32_t xs[kConsInFlight];
 #pragma unroll
-        for (int u = 0; u < kConsInFlight; u++)
-          xs[u] = (wv && i0 + u < nr) ? __ldg(words + (int64_t)srow[i0 + u] * Kw + w) : 0u;
+        for (int u = 0; u < kConsInFlight; u++) {
+          const int i = i0 + u * kConsGroups;
+          xs[u] = (wv && i < nr) ? __ldg(words + (int64_t)srow[i] * Kw + w) : 0u;
+        }
 #pragma unroll
         for (int u = 0; u < kConsInFlight; u++) {
           uint32_t x = xs[u];
 #pragma unroll
-          for (int p = 0; p < 32; p++) {
+          for (int p = 0; p < kConsPlanes; p++) {
             const uint32_t carry = plane[p] & x;
             plane[p] ^= x;
             x = carry;
@@ -374,29 +383,33 @@ __global__ void __launch_bounds__(kConsThreads) k_consensus(const uint32_t* __re
           }
         }
       }
-    }
-    uint32_t gt = 0u, eq = ~0u;  // count > half, count == half (so far, high planes first)
+      if (wv) {
+#pragma unroll 4
+        for (int b = 0; b < 32; b++) {
+          int cnt = 0;
 #pragma unroll
-    for (int p = 31; p >= 0; p--) {
-      if ((half >> p) & 1u) {
-        eq &= plane[p];
-      } else {
-        gt |= eq & plane[p];
-        eq &= ~plane[p];
+          for (int p = 0; p < kConsPlanes; p++) cnt |= (int)((plane[p] >> b) & 1u) << p;
+          if (cnt) atomicAdd(&colcnt[b * kConsWords + wl], cnt);
+        }
       }
     }
-    if (!wv) continue;
-    uint32_t m = gt;
-    cons[c * Kw + w] = m;
-    pop += __popc(m);
-    while (m) {
-      const int b = __ffs(m) - 1;
-      m &= m - 1;
-      const uint32_t k = (uint32_t)(w * 32 + b);
+    __syncthreads();
+    if (g == 0 && wv) {
+      uint32_t m = 0u;
+      for (int b = 0; b < 32; b++)
+        if (2 * colcnt[b * kConsWords + wl] > sz) m |= 1u << b;
+      cons[c * Kw + w] = m;
+      pop += __popc(m);
+      while (m) {
+        const int b = __ffs(m) - 1;
+        m &= m - 1;
+        const uint32_t k = (uint32_t)(w * 32 + b);
 #pragma unroll
-      for (int j = 0; j < kMaxHashes; j++)
-        if (j < H) mn[j] = min(mn[j], mix32(k, (uint32_t)j, seed));
+        for (int j = 0; j < kMaxHashes; j++)
+          if (j < H) mn[j] = min(mn[j], mix32(k, (uint32_t)j, seed));
+      }
     }
+    __syncthreads();  // colcnt is cleared for the next block of words
   }
 #pragma unroll
   for (int j = 0; j < kMaxHashes; j++) {
