@@ -24,42 +24,144 @@ size_t scan_workspace_bytes(int64_t n);
 
 namespace {
 
-// Every 8x8 tile: bitmap, and 1 / 0 for the compaction scan.
-__global__ void __launch_bounds__(256) k_tiles8_build(const uint32_t* __restrict__ words, int64_t M, int64_t Kw,
-                                                      int64_t Mt, int64_t Kt, uint64_t* __restrict__ all,
-                                                      int32_t* __restrict__ flag) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= Mt * Kt) return;
-  const int64_t ty = t / Kt, tx = t - ty * Kt;
-  uint64_t m = 0;
+// Packed rows -> 8x8 tiles in three passes over A's words.  Work unit: a
+// "quad" = word q of the 8 rows of tile row ty, i.e. the four tiles
+// tx = 4q..4q+3 (byte j of each row's word is tile 4q+j's row); quads in
+// (ty, q) order give tiles in ascending tile order.  A CTA takes kT8Span
+// consecutive quads, thread t the quads base + k*256 + t (k < kT8Quads), so
+// every load of a row's words is coalesced.
+//   1. per CTA: nonzero tiles and their set bits;
+//   2. one CTA scans both per-CTA totals (exclusive), writes *n_tiles;
+//   3. per CTA again: the tiles are rebuilt, placed by a block scan of the
+//      per-thread counts on top of the CTA's offsets, and written with their
+//      popcount offset; then offset[n..T] = nnz.
+// A's words are read twice; nothing of size T is written besides offset.
+constexpr int kT8Threads = 256;
+constexpr int kT8Quads = 4;
+constexpr int kT8Span = kT8Threads * kT8Quads;
+
+// 4x4 byte transpose: out[j] = bytes j of a, b, c, d (in that byte order).
+__device__ __forceinline__ void byte_transpose4(uint32_t a, uint32_t b, uint32_t c, uint32_t d, uint32_t (&out)[4]) {
+  const uint32_t ab_lo = __byte_perm(a, b, 0x5140), ab_hi = __byte_perm(a, b, 0x7362);  // a0 b0 a1 b1 / a2 b2 a3 b3
+  const uint32_t cd_lo = __byte_perm(c, d, 0x5140), cd_hi = __byte_perm(c, d, 0x7362);
+  out[0] = __byte_perm(ab_lo, cd_lo, 0x5410);
+  out[1] = __byte_perm(ab_lo, cd_lo, 0x7632);
+  out[2] = __byte_perm(ab_hi, cd_hi, 0x5410);
+  out[3] = __byte_perm(ab_hi, cd_hi, 0x7632);
+}
+
+// The four tiles of quad qd: tile j's byte r is byte j of row r's word.
+__device__ __forceinline__ void quad_tiles(const uint32_t* __restrict__ words, int64_t M, int64_t Kw, int64_t qd,
+                                           uint64_t (&m)[4]) {
+  const int64_t ty = qd / Kw, q = qd - ty * Kw;
+  uint32_t w[8];
 #pragma unroll
   for (int r = 0; r < 8; r++) {
     const int64_t row = ty * 8 + r;
-    if (row < M) {
-      const uint32_t w = __ldg(words + row * Kw + (tx >> 2));
-      m |= (uint64_t)((w >> (8 * (tx & 3))) & 0xffu) << (8 * r);
-    }
+    w[r] = row < M ? __ldg(words + row * Kw + q) : 0u;
   }
-  all[t] = m;
-  flag[t] = m != 0ull;
+  uint32_t lo[4], hi[4];
+  byte_transpose4(w[0], w[1], w[2], w[3], lo);
+  byte_transpose4(w[4], w[5], w[6], w[7], hi);
+#pragma unroll
+  for (int j = 0; j < 4; j++) m[j] = ((uint64_t)hi[j] << 32) | lo[j];
 }
 
-// Nonzero tiles to their compacted slots; pc[p] = popcount (pc zeroed first).
-__global__ void __launch_bounds__(256) k_tiles8_scatter(const uint64_t* __restrict__ all,
-                                                        const int32_t* __restrict__ pos, int64_t Kt, int64_t T,
-                                                        uint64_t* __restrict__ bmp, int32_t* __restrict__ trow,
-                                                        int32_t* __restrict__ tcol, int32_t* __restrict__ pc,
-                                                        int64_t* __restrict__ n_tiles) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t == 0) *n_tiles = pos[T];
-  if (t >= T) return;
-  const uint64_t m = all[t];
-  if (!m) return;
-  const int p = pos[t];
-  bmp[p] = m;
-  trow[p] = (int32_t)(t / Kt);
-  tcol[p] = (int32_t)(t % Kt);
-  pc[p] = __popcll(m);
+__global__ void __launch_bounds__(kT8Threads) k_t8_count(const uint32_t* __restrict__ words, int64_t M, int64_t Kw,
+                                                         int64_t Q, int32_t* __restrict__ cnt_blk,
+                                                         int32_t* __restrict__ pc_blk) {
+  __shared__ int sw[32];
+  int c = 0, pc = 0;
+  for (int k = 0; k < kT8Quads; k++) {
+    const int64_t qd = (int64_t)blockIdx.x * kT8Span + (int64_t)k * kT8Threads + threadIdx.x;
+    if (qd >= Q) break;
+    uint64_t m[4];
+    quad_tiles(words, M, Kw, qd, m);
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      c += m[j] != 0ull;
+      pc += __popcll(m[j]);
+    }
+  }
+  int tc, tp;
+  block_exclusive_scan(c, sw, &tc);
+  block_exclusive_scan(pc, sw, &tp);
+  if (threadIdx.x == 0) {
+    cnt_blk[blockIdx.x] = tc;
+    pc_blk[blockIdx.x] = tp;
+  }
+}
+
+// Exclusive scans of the per-CTA tile counts and popcounts, in place; the
+// totals go to *n_tiles and tot[0].
+__global__ void __launch_bounds__(1024) k_t8_scan(int32_t* __restrict__ cnt_blk, int32_t* __restrict__ pc_blk,
+                                                  int64_t nb, int64_t* __restrict__ n_tiles,
+                                                  int32_t* __restrict__ tot) {
+  __shared__ int sw[32];
+  int cc = 0, cp = 0;
+  for (int64_t b0 = 0; b0 < nb; b0 += 1024) {
+    const int64_t i = b0 + threadIdx.x;
+    const int c = i < nb ? cnt_blk[i] : 0, p = i < nb ? pc_blk[i] : 0;
+    int tc, tp;
+    const int ec = block_exclusive_scan(c, sw, &tc);
+    const int ep = block_exclusive_scan(p, sw, &tp);
+    if (i < nb) {
+      cnt_blk[i] = cc + ec;
+      pc_blk[i] = cp + ep;
+    }
+    cc += tc;
+    cp += tp;
+  }
+  if (threadIdx.x == 0) {
+    *n_tiles = cc;
+    tot[0] = cp;
+  }
+}
+
+__global__ void __launch_bounds__(kT8Threads) k_t8_write(const uint32_t* __restrict__ words, int64_t M, int64_t Kw,
+                                                         int64_t Q, int64_t Kt, int64_t T,
+                                                         const int32_t* __restrict__ cnt_off,
+                                                         const int32_t* __restrict__ pc_off,
+                                                         const int64_t* __restrict__ n_tiles,
+                                                         const int32_t* __restrict__ tot, uint64_t* __restrict__ bmp,
+                                                         int32_t* __restrict__ trow, int32_t* __restrict__ tcol,
+                                                         int32_t* __restrict__ offset) {
+  __shared__ int sw[32];
+  int run_c = cnt_off[blockIdx.x], run_p = pc_off[blockIdx.x];
+  for (int k = 0; k < kT8Quads; k++) {
+    const int64_t qd = (int64_t)blockIdx.x * kT8Span + (int64_t)k * kT8Threads + threadIdx.x;
+    uint64_t m[4] = {0ull, 0ull, 0ull, 0ull};
+    if (qd < Q) quad_tiles(words, M, Kw, qd, m);
+    int c = 0, pc = 0;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      c += m[j] != 0ull;
+      pc += __popcll(m[j]);
+    }
+    int tc, tp;
+    int pos = block_exclusive_scan(c, sw, &tc) + run_c;
+    int po = block_exclusive_scan(pc, sw, &tp) + run_p;
+    if (c) {
+      const int64_t ty = qd / Kw, q = qd - ty * Kw;
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        if (!m[j]) continue;
+        bmp[pos] = m[j];
+        trow[pos] = (int32_t)ty;
+        tcol[pos] = (int32_t)(4 * q + j);
+        offset[pos] = po;
+        pos++;
+        po += __popcll(m[j]);
+      }
+    }
+    run_c += tc;
+    run_p += tp;
+  }
+  // offset[t] = nnz for t in [n, T]
+  const int64_t n = *n_tiles;
+  const int32_t nnz = tot[0];
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t t = n + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t <= T; t += stride) offset[t] = nnz;
 }
 
 // Tile bytes back into packed rows (rows zeroed first).  Byte tx of a row's
@@ -174,9 +276,9 @@ __global__ void __launch_bounds__(256) k_csr_fill(const int32_t* __restrict__ ro
 }  // namespace
 
 size_t tiles8_workspace_bytes(int64_t M, int64_t K) {
-  const int64_t T = ceil_div(M, 8) * ceil_div(K, 8);
-  // all[T] u64, flag[T], pos[T+1], pc[T] int32, scan blocks
-  return (size_t)T * 8 + 3 * ((size_t)T + 1) * 4 + scan_workspace_bytes(T) + 4 * 256;
+  // per-CTA tile counts and popcounts, the nnz total
+  const int64_t nb = ceil_div(ceil_div(M, 8) * ceil_div(K, 32), kT8Span);
+  return 2 * ((size_t)nb * 4 + 256) + 256;
 }
 
 static inline uint8_t* carve(uint8_t*& p, size_t bytes) {
@@ -188,21 +290,17 @@ static inline uint8_t* carve(uint8_t*& p, size_t bytes) {
 int launch_rows_to_tiles8(const uint32_t* words, int64_t M, int64_t K, uint64_t* bmp, int32_t* trow, int32_t* tcol,
                           int32_t* offset, int64_t* n_tiles, void* ws, cudaStream_t s) {
   const int64_t Mt = ceil_div(M, 8), Kt = ceil_div(K, 8), T = Mt * Kt, Kw = ceil_div(K, 32);
+  const int64_t Q = Mt * Kw, nb = ceil_div(Q, kT8Span);
   uint8_t* p = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(ws) + 255) & ~(uintptr_t)255);
-  uint64_t* all = reinterpret_cast<uint64_t*>(carve(p, (size_t)T * 8));
-  int32_t* flag = reinterpret_cast<int32_t*>(carve(p, (size_t)T * 4));
-  int32_t* pos = reinterpret_cast<int32_t*>(carve(p, ((size_t)T + 1) * 4));
-  int32_t* pc = reinterpret_cast<int32_t*>(carve(p, ((size_t)T + 1) * 4));
-  void* sws = carve(p, scan_workspace_bytes(T));
-  const unsigned g = (unsigned)ceil_div(T, 256);
-  k_tiles8_build<<<g, 256, 0, s>>>(words, M, Kw, Mt, Kt, all, flag);
+  int32_t* cnt_blk = reinterpret_cast<int32_t*>(carve(p, (size_t)nb * 4));
+  int32_t* pc_blk = reinterpret_cast<int32_t*>(carve(p, (size_t)nb * 4));
+  int32_t* tot = reinterpret_cast<int32_t*>(p);
+  k_t8_count<<<(unsigned)nb, kT8Threads, 0, s>>>(words, M, Kw, Q, cnt_blk, pc_blk);
+  k_t8_scan<<<1, 1024, 0, s>>>(cnt_blk, pc_blk, nb, n_tiles, tot);
+  k_t8_write<<<(unsigned)nb, kT8Threads, 0, s>>>(words, M, Kw, Q, Kt, T, cnt_blk, pc_blk, n_tiles, tot, bmp, trow,
+                                                 tcol, offset);
   BSP_LAUNCHED();
-  BSP_TRY(launch_scan_i32(flag, T, pos, sws, s));
-  BSP_CUDA(cudaMemsetAsync(pc, 0, (size_t)T * 4, s));
-  k_tiles8_scatter<<<g, 256, 0, s>>>(all, pos, Kt, T, bmp, trow, tcol, pc, n_tiles);
-  BSP_LAUNCHED();
-  // offsets over all T slots: past the n-th they stay at the total
-  return launch_scan_i32(pc, T, offset, sws, s);
+  return BSP_OK;
 }
 
 int launch_tiles8_to_rows(const uint64_t* bmp, const int32_t* trow, const int32_t* tcol, int64_t n, int64_t M,
