@@ -467,8 +467,9 @@ __global__ void __launch_bounds__(tc_threads(TPS), 1) k_spmm_tc(TcArgs a, const 
 
   // ---------------- epilogue (producer warps) ----------------
   // Warp w reads TMEM lanes 32*(w%4).. (a warp may only touch its own
-  // quarter of the lanes) of accumulator (w/4)%2, columns 128*(w/8)..; a
-  // thread holds 32 columns of one output row at a time.  Products other
+  // quarter of the lanes) of accumulator (w/4)%2, column half w/8 of the
+  // tile's 64·nbox live columns (so a narrow tile keeps all 16 warps busy);
+  // a thread holds 32 columns of one output row at a time.  Products other
   // than the SDDMM pass them through a 32x32 tile of the (now idle) stage
   // memory, so that each store instruction writes four whole 128-byte rows
   // of C instead of 16 bytes in each of 32 rows.
@@ -489,13 +490,13 @@ __global__ void __launch_bounds__(tc_threads(TPS), 1) k_spmm_tc(TcArgs a, const 
     const bool split = gridDim.z > 1;
     float* cbase = split ? a.part + (int64_t)blockIdx.z * a.part_stride : gC;
     const int64_t cld = split ? a.ldp : gldc;
-    const int64_t ccol = col0 + cg * (kTcN / 2);  // the warp's first column
+    const int cspan = nbox * (kBoxCols / 2);      // live columns per column half (a multiple of 32)
+    const int64_t ccol = col0 + cg * cspan;         // the warp's first column
     const bool live = row < out_rows && wlive;
     const uint32_t* arow = gA + row * gKw;
-    const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * kTcN + cg * (kTcN / 2));
+    const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * kTcN + cg * cspan);
     float* tile = reinterpret_cast<float*>(sm.a) + warp * 32 * kEpiStride;
-    // columns of this warp's half that hold output: up to 64·nbox of the tile
-    const int c8_end = (int)max(0, min(kTcN / 2, nbox * kBoxCols - cg * (kTcN / 2))) / 8;
+    const int c8_end = cspan / 8;
     for (int c8 = 0; c8 < c8_end; c8 += 4) {
       uint32_t r[4][8];
       if (have && ok) {
