@@ -557,7 +557,7 @@ def run_batched(args):
            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "bf16", "data": "synthetic (seeded numpy, seed 7+i per problem)",
            "config": {"workload": "batched_512_N128_bf16", "problems": len(probs), "N": N,
-                      "nnz": nnz, "graph": "one launch (a CTA per 256x256 work item), graph-captured"},
+                      "nnz": nnz, "graph": "one persistent launch (a CTA per SM taking 256-row items from a device work queue), graph-captured"},
            "aggregate_gbs": ws * comp / (ms * 1e-3) / 1e9,
            "effective_tflops": 2.0 * nnz * N / (ms * 1e-3) / 1e12,
            "fp32_loop_ms": ms32, "speedup_vs_fp32_loop": ms32 / ms,

@@ -1,21 +1,26 @@
 // spmm_batched.cu — many independent bitmap SpMMs in one tensor-core launch.
 //
 // A batch (bsp_batch_create) holds, in device memory, one record per problem
-// (B's tensor map, encoded once on the host, and A, C, sizes) and a work list
+// (B's tensor map, encoded once on the host, and A, C, sizes), a work list
 // with one item per (problem, 256-row block, 256-column block), sorted by
-// reduction length, longest first, so the long items start in the first wave.
-// bsp_batched_spmm runs the list with the tensor-core SpMM kernel
-// (spmm_tc.cu, batch mode): one CTA per item, the item's problem read from
-// the record, every K tile of its rows (a batch has no occupancy plan), B
-// streamed by TMA through the problem's own tensor map.  One launch, no host
-// synchronisation, no allocation.
+// reduction length, longest first, and a work-queue counter.
+// bsp_batched_spmm runs the list in one launch, with no host synchronisation
+// and no allocation: for N ≤ 128 with the persistent kernel below (a CTA
+// per SM pulls items from the queue); for wider N with the tensor-core SpMM
+// kernel in batch mode (spmm_tc.cu: one CTA per item).  Both read the item's
+// problem from its record, run every K tile of its rows (a batch has no
+// occupancy plan) and stream B by TMA through the problem's own tensor map.
 #include <algorithm>
 #include <new>
+#include <type_traits>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
 #include "bsp_internal.cuh"
+#include "ptx.cuh"
 #include "spmm.cuh"
+#include "tc_common.cuh"
 
 namespace bsp {
 
@@ -33,7 +38,359 @@ int batched_device_error(int* out, bool clear) {
 
 namespace {
 constexpr int64_t kItemRows = 256, kItemCols = 256;  // the tensor-core kernel's CTA tile
+
+// ---- persistent batched kernel (N ≤ 128) ----------------------------------
+// One CTA per SM takes work items from a device-side queue (an atomic
+// counter over the longest-first item list) until the list is exhausted.
+// An item is 256 rows of one problem (two 128-row halves) times all N ≤ 128
+// columns, reduced over every 32-column K tile of its rows.  Roles:
+//   warps 0-7 (producers): thread r expands row r of both K tiles of a stage
+//     (2.0 per set bit, K-major core matrices), words loaded 4 stages ahead;
+//   warp 8 (TMA, lane 0): fetches the next item into a 4-slot ring in shared
+//     memory for every role, then loads each stage's B rows as 64x32 boxes
+//     (128-byte swizzle) through the problem's tensor map;
+//   warp 9 (MMA, lane 0): allocates TMEM, issues tcgen05.mma (M128 N≤128
+//     K16) into accumulator set j % 2 of item j and commits each stage to
+//     its "empty" barrier and each item to "tfull";
+//   warps 10-17 (epilogue): read set j % 2 back (warp w touches TMEM lanes
+//     32·(w%4)..; warps 10-13 and 14-17 split the columns), scale by 0.5,
+//     store C through a 32x32 staging tile per warp, then free the set
+//     ("tempty") and the item's ring slot ("qempty").
+// With two accumulator sets the epilogue of item j runs under the MMAs of
+// item j+1, and the producers and TMA run up to three stages ahead across
+// item boundaries, so an item costs its MMAs, not its set-up.  Stage and
+// item counters run over the whole launch, so every mbarrier phase follows
+// from a counter.  Every wait is bounded: on timeout the role records error
+// 4 in g_batch_error and stops; the others' bounded waits then end.
+constexpr int kPRows = 256, kPM = 128, kPK = 32, kPMaxN = 128;
+constexpr int kPTps = 2, kPStages = 3, kPQ = 4;
+constexpr int kPATile = kPRows * kPK * 2;  // 16 KB: both halves of one K tile
+constexpr int kPAHalf = kPM * kPK * 2;     // 8 KB
+constexpr int kPBox = 64 * kPK * 2;        // 4 KB: 64 columns x 32 rows
+constexpr int kPBTile = 2 * kPBox;         // 8 KB: up to 128 columns
+constexpr int kPAStage = kPTps * kPATile, kPBStage = kPTps * kPBTile;
+constexpr int kPProdWarps = kPRows / 32;  // 8
+constexpr int kPTmaWarp = kPProdWarps, kPMmaWarp = kPProdWarps + 1;
+constexpr int kPEpiWarp0 = kPProdWarps + 2, kPEpiWarps = 8;
+constexpr int kPThreads = (kPEpiWarp0 + kPEpiWarps) * 32;  // 576
+constexpr int kPEpiStride = 36;       // staging rows 36 floats apart (16-byte aligned, conflict-free)
+constexpr uint32_t kPTmemCols = 512;  // two sets x two halves x 128 columns
+constexpr int kPWordAhead = 4;
+constexpr int kPErr = 4;
+
+struct __align__(1024) PersistSmem {
+  uint8_t a[kPStages * kPAStage];  // 96 KB
+  uint8_t b[kPStages * kPBStage];  // 48 KB, 1 KB-aligned (128-byte swizzle atoms)
+  float epi[kPEpiWarps][32 * kPEpiStride];
+  uint64_t full[kPStages], empty[kPStages];
+  uint64_t tfull[2], tempty[2];
+  uint64_t qfull[kPQ], qempty[kPQ];
+  int qitem[kPQ];
+  uint32_t tmem_addr;
+};
+constexpr size_t kPSmemAlign = 1024;
+static_assert(sizeof(PersistSmem) + kPSmemAlign <= 232448, "persistent batched kernel: shared memory");
+
+__device__ __forceinline__ void persist_fail() { atomicCAS(&g_batch_error, 0, kPErr); }
+
+// lane 0 waits on `bar` (bounded) and reads *val; the warp gets both
+__device__ __forceinline__ bool warp_wait_read(uint64_t* bar, uint32_t parity, const int* val, int* out) {
+  int ok = 1, v = 0;
+  if ((threadIdx.x & 31) == 0) {
+    ok = ptx::mbar_wait(bar, parity) ? 1 : 0;
+    if (ok && val) v = *(volatile const int*)val;
+  }
+  ok = __shfl_sync(kFull, ok, 0);
+  if (out) *out = __shfl_sync(kFull, v, 0);
+  return ok != 0;
+}
+
+template <typename BT>
+__global__ void __launch_bounds__(kPThreads, 1)
+    k_batched_persist(const BatchProblemTc* __restrict__ probs, const int4* __restrict__ items, int n_items,
+                      int* next_item, int64_t N) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  PersistSmem& sm = *reinterpret_cast<PersistSmem*>(
+      smem_raw + ((kPSmemAlign - (ptx::smem_addr(smem_raw) & (kPSmemAlign - 1))) & (kPSmemAlign - 1)));
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nbox = (int)((min(N, (int64_t)kPMaxN) + 63) / 64);  // 64-column boxes holding output columns
+  if (tid == 0) {
+    for (int s = 0; s < kPStages; s++) {
+      ptx::mbar_init(&sm.full[s], kPProdWarps + 1);  // producer warps + the TMA transaction arrival
+      ptx::mbar_init(&sm.empty[s], 1);               // tcgen05.commit of the stage's MMAs
+    }
+    for (int b = 0; b < 2; b++) {
+      ptx::mbar_init(&sm.tfull[b], 1);
+      ptx::mbar_init(&sm.tempty[b], kPEpiWarps);
+    }
+    for (int q = 0; q < kPQ; q++) {
+      ptx::mbar_init(&sm.qfull[q], 1);
+      ptx::mbar_init(&sm.qempty[q], kPEpiWarps);
+    }
+    ptx::fence_mbar_init();
+  }
+  if (warp == kPMmaWarp) {
+    ptx::tmem_alloc(&sm.tmem_addr, kPTmemCols);
+    ptx::tmem_relinquish();
+  }
+  ptx::tc_fence_before_sync();
+  __syncthreads();
+  ptx::tc_fence_after_sync();
+  const uint32_t tmem = sm.tmem_addr;
+
+  if (warp < kPProdWarps) {
+    // ---------------- A producers ----------------
+    const int r = tid;  // row of the item
+    uint32_t g = 0;     // stages produced so far (whole launch)
+    for (int j = 0;; j++) {
+      int it = -1;
+      if (!warp_wait_read(&sm.qfull[j % kPQ], (uint32_t)(j / kPQ) & 1u, &sm.qitem[j % kPQ], &it)) {
+        if (lane == 0) persist_fail();
+        break;
+      }
+      if (it < 0) break;
+      const int4 w4 = __ldg(items + it);
+      const BatchProblemTc* p = probs + w4.x;
+      const uint32_t* A = p->A;
+      const int64_t M = p->M, Kw = p->Kw;
+      const int64_t arow = (int64_t)w4.y * kPRows + r;
+      const int nt = w4.w, nst = (nt + kPTps - 1) / kPTps;
+      auto load_word = [&](int k) -> uint32_t { return (k < nt && arow < M) ? __ldg(A + arow * Kw + k) : 0u; };
+      uint32_t wq[kPWordAhead][kPTps];
+#pragma unroll
+      for (int a = 0; a < kPWordAhead; a++)
+#pragma unroll
+        for (int u = 0; u < kPTps; u++) wq[a][u] = load_word(kPTps * a + u);
+      bool fail = false;
+      for (int i = 0; i < nst; i++, g++) {
+        const int s = (int)(g % kPStages);
+        uint32_t wn[kPTps];
+#pragma unroll
+        for (int u = 0; u < kPTps; u++) wn[u] = load_word(kPTps * (i + kPWordAhead) + u);
+        if (g >= (uint32_t)kPStages &&
+            !warp_wait_read(&sm.empty[s], ((g / kPStages) - 1) & 1u, nullptr, nullptr)) {
+          if (lane == 0) persist_fail();
+          fail = true;
+          break;
+        }
+#pragma unroll
+        for (int u = 0; u < kPTps; u++) {
+          if (kPTps * i + u >= nt) continue;
+          uint4 e[4];
+          tc::expand32_two(wq[0][u], e);
+          uint8_t* as = sm.a + s * kPAStage + u * kPATile + (r >> 3) * tc::kSbo + (r & 7) * 16;
+#pragma unroll
+          for (int c = 0; c < 4; c++) *reinterpret_cast<uint4*>(as + c * tc::kLbo) = e[c];
+        }
+        ptx::fence_proxy_async_smem();
+        __syncwarp();
+        if (lane == 0) ptx::mbar_arrive(&sm.full[s]);
+#pragma unroll
+        for (int a = 0; a < kPWordAhead - 1; a++)
+#pragma unroll
+          for (int u = 0; u < kPTps; u++) wq[a][u] = wq[a + 1][u];
+#pragma unroll
+        for (int u = 0; u < kPTps; u++) wq[kPWordAhead - 1][u] = wn[u];
+      }
+      if (fail) break;
+    }
+  } else if (warp == kPTmaWarp) {
+    // ---------------- item queue + B by TMA ----------------
+    if (lane == 0) {
+      const uint32_t b0 = ptx::smem_addr(sm.b), f0 = ptx::smem_addr(&sm.full[0]);
+      uint32_t g = 0;
+      for (int j = 0;; j++) {
+        const int q = j % kPQ;
+        if (j >= kPQ && !ptx::mbar_wait(&sm.qempty[q], (uint32_t)((j / kPQ) - 1) & 1u)) {
+          persist_fail();
+          break;
+        }
+        const int it = atomicAdd(next_item, 1);
+        sm.qitem[q] = it < n_items ? it : -1;
+        ptx::mbar_arrive(&sm.qfull[q]);
+        if (it >= n_items) break;
+        const int4 w4 = __ldg(items + it);
+        const void* map = &probs[w4.x].map;
+        ptx::tensormap_acquire(map);  // written by the host into global memory
+        const int nt = w4.w, nst = (nt + kPTps - 1) / kPTps;
+        bool fail = false;
+        for (int i = 0; i < nst; i++, g++) {
+          const int s = (int)(g % kPStages);
+          if (g >= (uint32_t)kPStages && !ptx::mbar_wait(&sm.empty[s], ((g / kPStages) - 1) & 1u)) {
+            persist_fail();
+            fail = true;
+            break;
+          }
+          const int cnt = min(kPTps, nt - kPTps * i);
+          ptx::mbar_arrive_expect_tx(&sm.full[s], (uint32_t)(cnt * nbox * kPBox));
+          for (int u = 0; u < cnt; u++) {
+            const int t = kPTps * i + u;
+            for (int jb = 0; jb < nbox; jb++)
+              ptx::tma_load_2d_u32(b0 + (uint32_t)(s * kPBStage + u * kPBTile + jb * kPBox), map, jb * 64, t * kPK,
+                                   f0 + (uint32_t)s * 8u);
+          }
+        }
+        if (fail) break;
+      }
+    }
+  } else if (warp == kPMmaWarp) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      const uint32_t ab = std::is_same<BT, __nv_bfloat16>::value ? 1u : 0u;
+      const uint32_t idesc = tc::idesc_f16(ab, 0u, 1u, (uint32_t)(nbox * 64), kPM);
+      const uint64_t adesc = ptx::smem_desc_noswizzle_u32(ptx::smem_addr(sm.a), tc::kLbo, tc::kSbo);
+      const uint64_t bdesc = ptx::smem_desc_noswizzle_u32(ptx::smem_addr(sm.b), kPBox, 1024) |
+                             ((uint64_t)tc::kLayoutSw128 << 61);
+      uint32_t g = 0;
+      for (int j = 0;; j++) {
+        if (!ptx::mbar_wait(&sm.qfull[j % kPQ], (uint32_t)(j / kPQ) & 1u)) {
+          persist_fail();
+          break;
+        }
+        const int it = *(volatile const int*)&sm.qitem[j % kPQ];
+        if (it < 0) break;
+        const int4 w4 = __ldg(items + it);
+        const int64_t M = probs[w4.x].M;
+        const int halves = (int64_t)w4.y * kPRows + kPM < M ? 3 : 1;
+        const int nt = w4.w, nst = (nt + kPTps - 1) / kPTps;
+        const int set = j & 1;
+        if (j >= 2 && !ptx::mbar_wait(&sm.tempty[set], (uint32_t)((j >> 1) - 1) & 1u)) {
+          persist_fail();
+          break;
+        }
+        ptx::tc_fence_after_sync();
+        const uint32_t dset = tmem + (uint32_t)(set * 256);
+        uint32_t started = 0;
+        bool fail = false;
+        for (int i = 0; i < nst; i++, g++) {
+          const int s = (int)(g % kPStages);
+          if (!ptx::mbar_wait(&sm.full[s], (g / kPStages) & 1u)) {
+            persist_fail();
+            fail = true;
+            break;
+          }
+          ptx::tc_fence_after_sync();
+#pragma unroll
+          for (int u = 0; u < kPTps; u++) {
+            if (kPTps * i + u >= nt) continue;
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+              if (!((halves >> h) & 1)) continue;
+#pragma unroll
+              for (int k = 0; k < 2; k++)  // K half k: A two core-matrix columns on, B two 8-row groups on
+                ptx::tc_mma_f16(dset + (uint32_t)(h * kPM),
+                                adesc + (uint64_t)((s * kPAStage + u * kPATile + h * kPAHalf + k * 2 * tc::kLbo) >> 4),
+                                bdesc + (uint64_t)((s * kPBStage + u * kPBTile + k * 2 * 1024) >> 4), idesc,
+                                ((started >> h) & 1u) || k > 0);
+              started |= 1u << h;
+            }
+          }
+          ptx::tc_commit(&sm.empty[s]);
+        }
+        if (fail) break;
+        if (nst > 0) ptx::tc_commit(&sm.tfull[set]);
+        else ptx::mbar_arrive(&sm.tfull[set]);
+      }
+    }
+  } else {
+    // ---------------- epilogue ----------------
+    const int e = warp - kPEpiWarp0;  // 0..7
+    const int q4 = warp & 3;          // the TMEM lane quarter this warp may access
+    const int ch = e >> 2;            // column half
+    const int cspan = nbox * 32;      // live columns per half (a multiple of 32)
+    float* tile = sm.epi[e];
+    for (int j = 0;; j++) {
+      int it = -1;
+      if (!warp_wait_read(&sm.qfull[j % kPQ], (uint32_t)(j / kPQ) & 1u, &sm.qitem[j % kPQ], &it)) {
+        if (lane == 0) persist_fail();
+        break;
+      }
+      if (it < 0) break;
+      const int4 w4 = __ldg(items + it);
+      const BatchProblemTc* p = probs + w4.x;
+      const int64_t M = p->M, ldc = p->ldc;
+      float* C = p->C;
+      const int nt = w4.w;
+      const int set = j & 1;
+      if (!warp_wait_read(&sm.tfull[set], (uint32_t)(j >> 1) & 1u, nullptr, nullptr)) {
+        if (lane == 0) persist_fail();
+        break;
+      }
+      ptx::tc_fence_after_sync();
+      for (int h = 0; h < 2; h++) {
+        const int64_t rbase = (int64_t)w4.y * kPRows + h * kPM + q4 * 32;  // the warp's first row
+        if (rbase >= M) continue;
+        const uint32_t tb = tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(set * 256 + h * kPM + ch * cspan);
+        for (int c8 = 0; c8 < cspan / 8; c8 += 4) {
+          uint32_t v[4][8];
+          if (nt > 0) {
+#pragma unroll
+            for (int u = 0; u < 4; u++) ptx::tmem_ld_32x32b_x8(tb + (uint32_t)((c8 + u) * 8), v[u]);
+            ptx::tmem_wait_ld();
+          } else {
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+#pragma unroll
+              for (int x = 0; x < 8; x++) v[u][x] = 0u;
+          }
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            float4* t4 = reinterpret_cast<float4*>(tile + lane * kPEpiStride + u * 8);
+            t4[0] = make_float4(__uint_as_float(v[u][0]) * tc::kTwoScale, __uint_as_float(v[u][1]) * tc::kTwoScale,
+                                __uint_as_float(v[u][2]) * tc::kTwoScale, __uint_as_float(v[u][3]) * tc::kTwoScale);
+            t4[1] = make_float4(__uint_as_float(v[u][4]) * tc::kTwoScale, __uint_as_float(v[u][5]) * tc::kTwoScale,
+                                __uint_as_float(v[u][6]) * tc::kTwoScale, __uint_as_float(v[u][7]) * tc::kTwoScale);
+          }
+          __syncwarp();
+          // 8 lanes per row: rows 4*k + lane/8, 16 bytes each
+          const int c4 = (lane & 7) * 4;
+          const int64_t gcol = (int64_t)ch * cspan + c8 * 8 + c4;
+#pragma unroll
+          for (int k = 0; k < 8; k++) {
+            const int jr = k * 4 + (lane >> 3);
+            const int64_t grow = rbase + jr;
+            if (grow < M && gcol < N)
+              *reinterpret_cast<float4*>(C + grow * ldc + gcol) = *reinterpret_cast<const float4*>(tile + jr * kPEpiStride + c4);
+          }
+          __syncwarp();
+        }
+      }
+      ptx::tc_fence_before_sync();
+      __syncwarp();
+      if (lane == 0) {
+        ptx::mbar_arrive(&sm.tempty[set]);
+        ptx::mbar_arrive(&sm.qempty[j % kPQ]);
+      }
+    }
+  }
+  ptx::tc_fence_before_sync();
+  __syncthreads();
+  if (warp == kPMmaWarp) {
+    ptx::tc_fence_after_sync();
+    ptx::tmem_dealloc(tmem, kPTmemCols);
+  }
+}
+
+template <typename BT>
+int launch_persist_t(const BatchProblemTc* probs, const int4* items, int n_items, int* counter, int64_t N,
+                     cudaStream_t st) {
+  constexpr size_t smem = sizeof(PersistSmem) + kPSmemAlign;
+  static bool configured[64] = {false};
+  int dev = 0;
+  BSP_CUDA(cudaGetDevice(&dev));
+  if (dev >= 64 || !configured[dev]) {
+    BSP_CUDA(cudaFuncSetAttribute(k_batched_persist<BT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (dev < 64) configured[dev] = true;
+  }
+  BSP_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), st));
+  const int grid = std::min(num_sms(), n_items);
+  k_batched_persist<BT><<<grid, kPThreads, smem, st>>>(probs, items, n_items, counter, N);
+  BSP_LAUNCHED();
+  return BSP_OK;
+}
+
 }  // namespace
+
 
 }  // namespace bsp
 
@@ -43,9 +400,10 @@ struct bsp_batch {
   int bdt = BSP_BF16;
   int n_items = 0;
   int device = 0;
-  void* dev = nullptr;  // BatchProblemTc[n] followed by int4 items[n_items]
+  void* dev = nullptr;  // BatchProblemTc[n], int4 items[n_items], the work-queue counter
   bsp::BatchProblemTc* probs = nullptr;
   int4* items = nullptr;
+  int* counter = nullptr;  // next item of the persistent kernel (reset by every run)
 };
 
 extern "C" {
@@ -97,7 +455,8 @@ int bsp_batch_create(const bsp_problem* problems, int n, int64_t N, int b_dtype,
   const size_t pbytes = sizeof(BatchProblemTc) * (size_t)std::max(n, 1);
   const size_t ibytes = sizeof(int4) * std::max<size_t>(items.size(), 1);
   const size_t poff = (pbytes + 255) & ~size_t(255);
-  cudaError_t e = cudaMalloc(&b->dev, poff + ibytes);
+  const size_t coff = poff + ((ibytes + 255) & ~size_t(255));
+  cudaError_t e = cudaMalloc(&b->dev, coff + 256);
   if (e != cudaSuccess) {
     cuda_status(e);
     delete b;
@@ -105,6 +464,7 @@ int bsp_batch_create(const bsp_problem* problems, int n, int64_t N, int b_dtype,
   }
   b->probs = static_cast<BatchProblemTc*>(b->dev);
   b->items = reinterpret_cast<int4*>(static_cast<char*>(b->dev) + poff);
+  b->counter = reinterpret_cast<int*>(static_cast<char*>(b->dev) + coff);
   const cudaStream_t s = (cudaStream_t)stream;
   int st = BSP_OK;
   if (n > 0 &&
@@ -137,7 +497,16 @@ int bsp_batched_spmm(const bsp_batch* b, bsp_stream_t stream) {
   cudaGetDevice(&dev);
   if (dev != b->device) return BSP_ERR_INVALID_ARG;
   if (b->n_items == 0 || b->N == 0) return BSP_OK;
-  return launch_batched_tc(b->probs, b->items, b->n_items, b->N, b->bdt, (cudaStream_t)stream);
+  const cudaStream_t s = (cudaStream_t)stream;
+  // N ≤ 128: the persistent kernel (BSP_BATCH_PERSIST=0 selects the CTA-per-item
+  // launch, for comparisons); wider N: a CTA per (256-row, 256-column) item
+  const char* e = getenv("BSP_BATCH_PERSIST");
+  if (b->N <= kPMaxN && !(e && e[0] == '0')) {
+    if (b->bdt == BSP_BF16) return launch_persist_t<__nv_bfloat16>(b->probs, b->items, b->n_items, b->counter, b->N, s);
+    if (b->bdt == BSP_F16) return launch_persist_t<__half>(b->probs, b->items, b->n_items, b->counter, b->N, s);
+    return BSP_ERR_UNSUPPORTED;
+  }
+  return launch_batched_tc(b->probs, b->items, b->n_items, b->N, b->bdt, s);
 }
 
 }  // extern "C"

@@ -394,8 +394,10 @@ def csr_to_tiled(row_ptr, col_idx, M, K, tile_rows, tile_cols, values=None):
 
 
 class Batch:
-    """Many independent C_i = A_i·B_i (16-bit B, shared N) in one persistent
-    tensor-core launch.  ``problems``: list of (words, K, B, C) tensors; the
+    """Many independent C_i = A_i·B_i (16-bit B, shared N) in one tensor-core
+    launch: for N ≤ 128 a persistent kernel (a CTA per SM, 256-row items from
+    a device work queue), otherwise a CTA per 256x256 item.  Runs of one
+    batch must not overlap on the GPU (they share the queue and the C buffers).  ``problems``: list of (words, K, B, C) tensors; the
     tensors are referenced by the batch and must outlive it."""
 
     def __init__(self, problems):

@@ -1,4 +1,4 @@
-"""Batched persistent tensor-core SpMM against the oracle: problems of uneven
+"""Batched tensor-core SpMM (persistent for N ≤ 128) against the oracle: problems of uneven
 M, K and density, column blocking, empty problems and CUDA-graph replay.
 Scaled error against FP64 ≤ 1e-4 (BF16 products are exact, FP32
 accumulation), integer-valued B exact."""
@@ -92,3 +92,39 @@ def test_batched_empty_reduction_and_validation():
     Bodd = torch.zeros((dev[0][1], 12), dtype=torch.bfloat16, device="cuda")
     with pytest.raises(capi.BspError):
         ops.Batch([(dev[0][0], dev[0][1], Bodd, torch.zeros((dev[0][0].shape[0], 12), device="cuda"))])
+
+
+_PATHS = r"""
+import sys, hashlib
+import numpy as np, torch
+sys.path.insert(0, sys.argv[1]); sys.path.insert(0, sys.argv[1] + "/tests")
+import test_gpu_batched as T
+from bitwise_spgemm_gb300 import capi, ops
+for N in (128, 72, 8):
+    probs = T._problems(40, N, seed=100 + N)
+    dev = T._run(probs, N)
+    batch = ops.Batch(dev)
+    batch.run()
+    batch.run()  # a second run: the work queue restarts
+    torch.cuda.synchronize()
+    assert capi.device_status() == 0
+    print(N, hashlib.sha1(b"".join(c.cpu().numpy().tobytes() for _, _, _, c in dev)).hexdigest())
+"""
+
+
+def test_persistent_matches_item_per_cta():
+    """N ≤ 128 runs on the persistent kernel (work queue, two TMEM
+    accumulator sets); the CTA-per-item launch computes the same MMAs in the
+    same order, so both give the same C bit for bit (ragged M, N = 72 and 8,
+    some problems with one 128-row half)."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    outs = []
+    for persist in ("1", "0"):
+        env = dict(os.environ, BSP_BATCH_PERSIST=persist)
+        r = subprocess.run([sys.executable, "-c", _PATHS, root], env=env, capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, r.stderr[-2000:]
+        outs.append(r.stdout.strip().splitlines()[-3:])
+    assert outs[0] == outs[1]
