@@ -725,13 +725,25 @@ def run_next(args):
         a = torch.from_numpy(cfg["a_words"].view(np.int32)).to(dev)
         b = torch.from_numpy(cfg["b_words"].view(np.int32)).to(dev)
         out = torch.empty(M, (N + 31) // 32, dtype=torch.int32, device=dev)
-        step = lambda: ops.symbolic_rows(a, K, b, N, out=out)
+        out_walk = torch.empty_like(out)
+        # the plan of A (built once, before the timed region, as for the SpMM)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        plan = ops.Plan(a, K)
+        torch.cuda.synchronize()
+        plan_ms = (time.perf_counter() - t0) * 1e3
+        pinfo = plan.info()
+        wsp = ops._ws("bsp_symbolic_workspace", plan._h, N, device=dev)
+        step = lambda: ops.symbolic_rows(a, K, b, N, out=out, plan=plan, workspace=wsp)
+        step_walk = lambda: ops.symbolic_rows(a, K, b, N, out=out_walk)
         if sampler:
             sampler.start()
         barrier(ws)
         ms = max_over_ranks(ws, _timed(step, steps, warm))
         barrier(ws)
         clocks = sampler.stop() if sampler else None
+        ms_walk = _timed(step_walk, max(3, steps // 4), 2)
+        same = bool(torch.equal(out, out_walk))
         ms_group = _timed(lambda: ops.group_rows(out, 512, 2), 3, 1)
         nnz = int(np.unpackbits(cfg["a_words"].view(np.uint8)).sum())
         comp = 3 * M * ((N + 31) // 32) * 4
@@ -740,13 +752,17 @@ def run_next(args):
         line = dict(base, metric="symbolic output mask GB/s (A+B+C words / time)", value=comp / (ms * 1e-3) / 1e9,
                     unit="GB/s", ms_per_step=ms, dtype="u32",
                     config={"workload": cfg["name"], "M": M, "K": K, "N": N, "nnz_A": nnz,
+                            "plan": "prototype plan of A built before the timed region (plan_ms)",
+                            "plan_ms": plan_ms, "n_proto": pinfo["n_proto"], "delta_nnz": pinfo["delta_nnz"],
                             "l2": "B's words (8 MiB) stay in L2; the gathers are L2 reads"},
-                    gather_gbs=gather / (ms * 1e-3) / 1e9, grouping_ms=ms_group,
+                    walk_ms=ms_walk, walk_gather_gbs=gather / (ms_walk * 1e-3) / 1e9,
+                    speedup_vs_walk=ms_walk / ms, planned_equals_walk=same, grouping_ms=ms_group,
                     roofline={"bound": "hbm", "achieved": comp / (ms * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
                               "frac": comp / (ms * 1e-3) / 1e9 / hbm, "traffic": None, "peak_source": hkind},
                     cpu_baseline={"value": comp / sec / 1e9, "unit": "GB/s", "cores": 1, "kind": "port",
                                   "sample": "oracle symbolic pass on the first %d rows, scaled to %d" % (rows, M)},
                     clocks=clocks)
+        plan.close()
     elif args.config == "f2":
         cfg = W.config_int8()
         M, K, N = cfg["M"], cfg["K"], cfg["N"]

@@ -80,6 +80,8 @@ SIGNATURES = {
     "bsp_spmm_t": [_P, _I64, _I64, _P, _I, _I64, _I64, _P, _I64, _P, _P, _SZ, _P],
     "bsp_sddmm": [_P, _I64, _I64, _P, _I64, _P, _I64, _I, _I64, _P, _I64, _P, _P],
     "bsp_symbolic_rows": [_P, _I64, _I64, _P, _I64, _P, _P],
+    "bsp_symbolic_workspace": [_P, _I64, _P],
+    "bsp_symbolic_rows_planned": [_P, _I64, _I64, _P, _I64, _P, _P, _P, _SZ, _P],
     "bsp_bitplane_spmm": [_P, _I, _I, _I64, _I64, _P, _I, _I64, _I64, _P, _I64, _P],
     "bsp_spmm_i8_workspace": [_I64, _I64, C.POINTER(_SZ)],
     "bsp_spmm_workspace_preferred": [_P, _I64, C.POINTER(_SZ)],

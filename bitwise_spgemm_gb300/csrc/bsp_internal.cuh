@@ -121,6 +121,12 @@ int launch_csr_to_tiled(const int32_t* row_ptr, const int32_t* col, const void* 
 // output.cu
 int launch_symbolic_rows(const uint32_t* A, int64_t M, int64_t K, const uint32_t* Bw, int64_t N, uint32_t* Cw,
                          cudaStream_t s);
+// Through a prototype plan: per-cluster bit-sliced column counts in
+// `planes` (symbolic_planes_bytes), then the rows from their deltas.
+size_t symbolic_planes_bytes(int64_t n_proto, int64_t N);
+int launch_symbolic_planned(const uint32_t* A, int64_t M, int64_t K, const uint32_t* Bw, int64_t N, uint32_t* Cw,
+                            const int32_t* row_cluster, const int32_t* delta_ptr, const uint32_t* delta_idx,
+                            const uint32_t* cons, int64_t n_proto, uint32_t* planes, cudaStream_t s);
 int launch_bitplane_spmm(const uint32_t* planes, int nplanes, int signed_top, int64_t M, int64_t K,
                          const void* B, int bdt, int64_t ldb, int64_t N, float* C, int64_t ldc, bool vec,
                          cudaStream_t s);

@@ -474,6 +474,38 @@ int bsp_symbolic_rows(const uint32_t* A_words, int64_t M, int64_t K, const uint3
   return launch_symbolic_rows(A_words, M, K, B_words, N, C_words, s);
 }
 
+// The planned form needs a prototype plan for this A, counts below 2^16
+// (K < 65536) and the workspace for the cluster planes; otherwise the walk.
+static bool symbolic_planned_ok(const bsp_plan* plan, int64_t M, int64_t K) {
+  return plan && plan->mode == BSP_PLAN_PROTO && plan->n_proto > 0 && plan->M == M && plan->K == K && K < 65536;
+}
+
+int bsp_symbolic_workspace(const bsp_plan* plan, int64_t N, size_t* bytes) {
+  if (!bytes || N < 0) return BSP_ERR_INVALID_ARG;
+  *bytes = 0;
+  if (plan && plan->mode == BSP_PLAN_PROTO && plan->n_proto > 0 && plan->K < 65536)
+    *bytes = symbolic_planes_bytes(plan->n_proto, N) + 256;
+  return BSP_OK;
+}
+
+int bsp_symbolic_rows_planned(const uint32_t* A_words, int64_t M, int64_t K, const uint32_t* B_words, int64_t N,
+                              uint32_t* C_words, const bsp_plan* plan, void* workspace, size_t workspace_bytes,
+                              bsp_stream_t stream) {
+  BSP_TRY(check_dims(M, K));
+  if (N < 0 || N > kMaxCols) return BSP_ERR_INVALID_ARG;
+  if (plan && (plan->M != M || plan->K != K)) return BSP_ERR_INVALID_ARG;
+  if (plan && plan->device != current_device()) return BSP_ERR_INVALID_ARG;
+  if (!symbolic_planned_ok(plan, M, K) || M == 0 || N == 0 || K == 0)
+    return bsp_symbolic_rows(A_words, M, K, B_words, N, C_words, stream);
+  if (!C_words || !A_words || !B_words) return BSP_ERR_INVALID_ARG;
+  if (!is_aligned(A_words, 4) || !is_aligned(B_words, 4) || !is_aligned(C_words, 4)) return BSP_ERR_ALIGNMENT;
+  const size_t need = symbolic_planes_bytes(plan->n_proto, N) + 256;
+  if (!workspace || workspace_bytes < need) return BSP_ERR_WORKSPACE;
+  uint32_t* planes = reinterpret_cast<uint32_t*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255));
+  return launch_symbolic_planned(A_words, M, K, B_words, N, C_words, plan->row_cluster, plan->delta_ptr,
+                                 plan->delta_idx, plan->cons, plan->n_proto, planes, (cudaStream_t)stream);
+}
+
 static bool layout16(const void* p, int64_t ld, int esz, int64_t N, int vcols);
 
 int bsp_bitplane_spmm(const uint32_t* planes, int n_planes, int is_signed, int64_t M, int64_t K, const void* B,

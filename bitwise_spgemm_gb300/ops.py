@@ -240,17 +240,25 @@ def tune(words, K, B, plan, out=None, workspace=None):
             "ms": best.ms}
 
 
-def symbolic_rows(a_words, K, b_words, N, out=None):
+def symbolic_rows(a_words, K, b_words, N, out=None, plan=None, workspace=None):
     """Bit pattern of A·B for two bit matrices: row i of the result [M,
     ceil(N/32)] is the OR of B's row masks at A's set bits.  The symbolic
     half of pre_spgemm (reference source/src/transform.cuh:1028-1057);
-    group_rows on the result is its output grouping."""
+    group_rows on the result is its output grouping.  With a prototype plan
+    of A the rows come from their clusters' counts and delta lists (same
+    result)."""
     M = a_words.shape[0]
     if b_words.shape[0] != K:
         raise ValueError("b_words must have K rows")
     if out is None:
         out = torch.empty((M, words_per_row(N)), dtype=torch.int32, device=a_words.device)
-    call("bsp_symbolic_rows", _p(a_words), M, K, _p(b_words), N, _p(out), _stream())
+    if plan is not None:
+        if workspace is None:
+            workspace = _ws("bsp_symbolic_workspace", plan._h, N, device=a_words.device)
+        call("bsp_symbolic_rows_planned", _p(a_words), M, K, _p(b_words), N, _p(out), plan._h, _p(workspace),
+             workspace.numel(), _stream())
+    else:
+        call("bsp_symbolic_rows", _p(a_words), M, K, _p(b_words), N, _p(out), _stream())
     return out
 
 

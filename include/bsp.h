@@ -346,6 +346,23 @@ int bsp_symbolic_rows(const uint32_t* A_words, int64_t M, int64_t K,
                       const uint32_t* B_words, int64_t N, uint32_t* C_words,
                       bsp_stream_t stream);
 
+/* The same mask through a prototype plan of A (bsp_plan_create).  A row of
+ * cluster c counts, per output column, the set bits of its columns' B masks
+ * as its cluster's counts (bit-sliced, from the consensus columns) plus its
+ * added columns minus its removed ones, and keeps the columns with a
+ * nonzero count; rows without a cluster OR their masks.  The result is
+ * identical to bsp_symbolic_rows.  Workspace: bsp_symbolic_workspace bytes
+ * (the clusters' count planes).  A plan that is not a prototype plan, or
+ * K ≥ 65536, runs bsp_symbolic_rows.  Same reference step as
+ * bsp_symbolic_rows (transform.cuh:1028-1057); the plan has no counterpart
+ * there. */
+int bsp_symbolic_workspace(const bsp_plan* plan, int64_t N, size_t* bytes);
+int bsp_symbolic_rows_planned(const uint32_t* A_words, int64_t M, int64_t K,
+                              const uint32_t* B_words, int64_t N,
+                              uint32_t* C_words, const bsp_plan* plan,
+                              void* workspace, size_t workspace_bytes,
+                              bsp_stream_t stream);
+
 /* Bit-plane product: C[M×N] (FP32, row stride ldc) = Σ_b w_b·(P_b·B) for the
  * planes P_b (0 ≤ b < n_planes ≤ 8) of an M×K 8-bit matrix, packed as
  * bsp_bitplanes writes them (planes[b][M][ceil(K/32)], LSB-first), with

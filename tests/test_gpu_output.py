@@ -29,6 +29,29 @@ def test_symbolic_rows_match_oracle(M, K, N, pa, pb):
     assert np.array_equal(got, W.pack_bits(prod))
 
 
+@pytest.mark.parametrize("N,pb", [(31, 0.05), (2056, 0.01), (8192, 0.002), (300, 0.3)])
+def test_symbolic_rows_through_plan(N, pb):
+    """Clustered A (plus rows that fit no cluster): the planned pass — the
+    clusters' bit-sliced counts, then each row's added and removed columns —
+    gives the same masks as the direct OR walk and the oracle, including
+    dense B masks where counts run high and removed columns matter."""
+    from bitwise_spgemm_gb300 import capi
+    rng = np.random.default_rng(N)
+    A, _, _ = W.clustered_bits(1500, 2500, n_proto=7, p_proto=0.08, p_flip=0.006, seed_proto=N, seed_rows=N + 1)
+    A[::13] = rng.random((A[::13].shape[0], 2500)) < 0.03  # rows that fit no cluster
+    A[5] = False                                             # an empty row
+    Bm = rng.random((2500, N)) < pb
+    a, b = W.pack_bits(A), W.pack_bits(Bm)
+    ad, bd = words_dev(a), words_dev(b)
+    plan = ops.Plan(ad, 2500, mode=capi.PLAN_PROTO)
+    info = plan.info()
+    assert info["mode"] == capi.PLAN_PROTO and info["direct_rows"] > 0 and info["delta_nnz"] > 0
+    got = words_host(ops.symbolic_rows(ad, 2500, bd, N, plan=plan))
+    assert np.array_equal(got, words_host(ops.symbolic_rows(ad, 2500, bd, N)))
+    assert np.array_equal(got, O.symbolic_rows(a, 2500, b, N))
+    assert capi.device_status() == 0
+
+
 @pytest.mark.parametrize("TR,G", [(512, 2), (64, 4)])
 def test_output_grouping_of_symbolic_masks(TR, G):
     # pre_spgemm's second half: first-fit grouping of the output rows
