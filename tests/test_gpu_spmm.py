@@ -291,3 +291,27 @@ def test_minhash_paths_agree():
         outs.append(json.loads(r.stdout.strip().splitlines()[-1]))
     assert outs[0] == outs[1]
     assert outs[0]["info"]["mode"] == capi.PLAN_PROTO
+
+
+def test_plan_with_many_rows():
+    """More than 32768 rows: the plan numbers its clusters and sizes its row
+    lists with the multi-CTA scans.  Integer B through the plan is exact, and
+    the planned symbolic mask equals the walk."""
+    rng = np.random.default_rng(77)
+    M, K, N = 40000, 512, 64
+    A, _, _ = W.clustered_bits(M, K, n_proto=20, p_proto=0.1, p_flip=0.004, seed_proto=77, seed_rows=78)
+    A[::101] = rng.random((A[::101].shape[0], K)) < 0.05
+    words = W.pack_bits(A)
+    wd = words_dev(words)
+    plan = ops.Plan(wd, K, mode=capi.PLAN_PROTO)
+    info = plan.info()
+    assert info["mode"] == capi.PLAN_PROTO and info["n_proto"] >= 20 and info["delta_nnz"] > 0
+    Bi = rng.integers(-8, 9, (K, N)).astype(np.float32)
+    C = ops.spmm(wd, K, torch.from_numpy(Bi).cuda(), plan=plan).cpu().numpy()
+    assert np.array_equal(C.astype(np.float64), O.spmm_f64(words, K, Bi))
+    Bm = W.pack_bits(rng.random((K, 96)) < 0.05)
+    bd = words_dev(Bm)
+    s1 = ops.symbolic_rows(wd, K, bd, 96, plan=plan)
+    s0 = ops.symbolic_rows(wd, K, bd, 96)
+    assert torch.equal(s1, s0)
+    assert capi.device_status() == 0
