@@ -316,21 +316,24 @@ def run_ours(args):
     d_C = [torch.empty((M, N), device=dev) for _ in range(2)]
     side = torch.cuda.Stream(device=dev)
     d2h = torch.cuda.Stream(device=dev)
-    downloaded = [torch.cuda.Event() for _ in range(2)]
+    downloaded = [torch.cuda.Event() for _ in range(2)]  # set j's C is on the host
+    used = [torch.cuda.Event() for _ in range(2)]        # set j's SpMM has run
 
     def e2e_step(i, reuse_plan):
-        # A's words first (the plan needs them); B goes up on a side stream
-        # while the plan is built, and the SpMM waits for that copy
+        # A's words first (the plan needs them); B goes up at the same time on
+        # a side stream, once the SpMM that last read this buffer has run, and
+        # the SpMM waits for that copy
         j = i % 2
         cur = torch.cuda.current_stream()
         cur.wait_event(downloaded[j])  # this buffer set's previous C is on the host
         d_words[j].copy_(h_words, non_blocking=True)
-        side.wait_stream(cur)
+        side.wait_event(used[j])
         with torch.cuda.stream(side):
             d_B[j].copy_(h_B, non_blocking=True)
         p = plan if reuse_plan else ops.Plan(d_words[j], K)
         cur.wait_stream(side)
         ops.spmm(d_words[j], K, d_B[j], plan=p, out=d_C[j], workspace=wsp if reuse_plan else None)
+        used[j].record(cur)
         if not reuse_plan:
             p.close_async()
         d2h.wait_stream(cur)
