@@ -261,9 +261,12 @@ typedef struct bsp_batch bsp_batch;
 int bsp_batch_create(const bsp_problem* problems, int n, int64_t N,
                      int b_dtype, bsp_batch** batch, bsp_stream_t stream);
 int bsp_batch_destroy(bsp_batch* batch);
-/* Every problem of the batch in one tensor-core launch, one CTA per work
- * item (no host synchronisation, no allocation: can be captured in a CUDA
- * graph).                                                                  */
+/* Every problem of the batch in one tensor-core launch, with no host
+ * synchronisation and no allocation; it can be captured in a CUDA graph.
+ * For N ≤ 128 the launch is persistent: a CTA per SM takes items from a
+ * work queue in the batch's device memory, which a memset in the same stream
+ * resets first.  For wider N it is one CTA per work item.  Runs of one batch
+ * must not overlap on the GPU: they share the queue and the C buffers.     */
 int bsp_batched_spmm(const bsp_batch* batch, bsp_stream_t stream);
 
 /* ======================================================================== */
