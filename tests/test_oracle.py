@@ -258,3 +258,28 @@ def test_csr_to_tiled_oracle_matches_csr2tiledcsr(M, K, TR, TC, shuffle):
         rows = np.array([e[0] for e in b], np.int64)
         exp = [int((rows < j).sum()) for j in range(TR + 1)]
         assert np.array_equal(toff[t], exp)
+
+
+def test_symbolic_mask_from_cluster_counts():
+    """The identity behind the planned symbolic pass, in numpy: for a row
+    with consensus c, added columns (row and not c) and removed columns (c
+    and not row), the per-column count of the row's B masks is
+    count(c) + count(added) - count(removed); it never drops below zero on
+    the way (removed columns are all in c), and its nonzeros are the OR mask
+    of the walk."""
+    import numpy as np
+    from bitwise_spgemm_gb300 import workloads as W
+    rng = np.random.default_rng(3)
+    A, _, near = W.clustered_bits(200, 300, n_proto=4, p_proto=0.1, p_flip=0.02, seed_proto=3, seed_rows=4)
+    Bm = (rng.random((300, 90)) < 0.05).astype(np.int64)
+    cons = np.stack([A[near == c].mean(axis=0) > 0.5 for c in range(4)])  # majority per cluster
+    Ai = A.astype(np.int64)
+    for i in range(A.shape[0]):
+        c = cons[near[i]]
+        add = (A[i] & ~c).astype(np.int64)
+        rem = (c & ~A[i]).astype(np.int64)
+        n_c = c.astype(np.int64) @ Bm
+        assert np.all(n_c - rem @ Bm >= 0)
+        n = n_c + add @ Bm - rem @ Bm
+        assert np.array_equal(n, Ai[i] @ Bm)
+        assert np.array_equal(n > 0, (Ai[i][:, None] * Bm).max(axis=0) > 0)
