@@ -161,7 +161,7 @@ __global__ void __launch_bounds__(kSymCWords * kSymCGroups) k_sym_cluster_planes
 // One warp per (row of C, 64-word chunk): clustered rows start from their
 // cluster's planes and apply their delta rows; other rows OR the masks of
 // their set bits.
-__global__ void __launch_bounds__(256) k_sym_rows_planned(const uint32_t* __restrict__ A, int64_t M, int64_t K,
+__global__ void __launch_bounds__(256, 4) k_sym_rows_planned(const uint32_t* __restrict__ A, int64_t M, int64_t K,
                                                           int64_t Kw, const uint32_t* __restrict__ Bw, int64_t Nw,
                                                           const int32_t* __restrict__ row_cluster,
                                                           const int32_t* __restrict__ delta_ptr,
