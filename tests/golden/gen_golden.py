@@ -96,6 +96,80 @@ def main():
     fx["check_bad"] = np.bool_(R.check(A01.astype(np.float32), Bn, Cbad))
     fx["check_C_bad"] = Cbad
 
+    # The sections below draw from their own generator, so the keys above keep their values.
+    rng = np.random.default_rng(20261204)
+
+    # 8. csr2tiledcsr (main.cu:499-588), three tile shapes; empty rows, an empty
+    #    tile and entries within a row in CSR (column) order
+    for name, (M, K, th, tw, p) in {"256x256": (768, 512, 256, 256, 0.03),
+                                    "64x64": (192, 128, 64, 64, 0.08),
+                                    "32x128": (96, 384, 32, 128, 0.05)}.items():
+        A = rng.random((M, K)) < p
+        A[5] = False
+        A[:th, :tw] = False  # tile 0 empty
+        rp = np.concatenate([[0], np.cumsum(A.sum(1))]).astype(np.int32)
+        col = np.nonzero(A)[1].astype(np.int32)
+        val = rng.standard_normal(len(col)).astype(np.float32)
+        t = R.csr2tiledcsr(rp, col, val, M, K, th, tw)
+        fx["c2t_%s_row_ptr" % name] = rp
+        fx["c2t_%s_col" % name] = col
+        fx["c2t_%s_val" % name] = val
+        fx["c2t_%s_shape" % name] = np.array([M, K, th, tw], np.int32)
+        for k in ("tile_nnz_acc", "tiled_offset", "tiled_col", "tiled_val", "tile_row_nnz"):
+            fx["c2t_%s_%s" % (name, k)] = t[k]
+
+    # 9. pre_spgemm (transform.cuh:984-1157): the symbolic output mask of A·B
+    #    with B a bitmap, and first-fit grouping of the output rows (2 groups).
+    #    TILE_HEIGHT = SPLIT_K = K (the kernel's only race-free shape, see
+    #    oracle/ref_emu_out.cpp); dense enough that rows spill.
+    for name, (M, N, t, pa, pb) in {"256": (512, 128, 256, 0.02, 0.05),
+                                    "64": (256, 96, 64, 0.05, 0.1)}.items():
+        K = t
+        A = rng.random((M, K)) < pa
+        A[7] = False
+        Bd = (rng.random((K, N)) < pb).astype(np.float32)
+        bw = R.dense2bitmask(Bd, 64)  # B's masks as main() builds them (MSB-first)
+        rp = np.concatenate([[0], np.cumsum(A.sum(1))]).astype(np.int32)
+        col = np.nonzero(A)[1].astype(np.int32)
+        tl = R.csr2tiledcsr(rp, col, np.ones(len(col), np.float32), M, K, t, t)
+        o = R.pre_spgemm(bw, tl, M, K, N, t)
+        fx["pre_%s_A_words" % name] = W.pack_bits(A)
+        fx["pre_%s_B_words_msb" % name] = bw
+        fx["pre_%s_shape" % name] = np.array([M, K, N, t], np.int32)
+        fx["pre_%s_c_bits" % name] = o["c_bits"]
+        fx["pre_%s_group_idx" % name] = o["group_idx"]
+        fx["pre_%s_group_mask" % name] = o["group_mask"]
+        fx["pre_%s_nnz" % name] = o["nnz"]
+
+    # 10. coo2bmp_noTuple_d (main.cu:692-779, mm.h:83-144): 8x8 bitmap tiles,
+    #     tile coordinates and popcount offsets, from COO entries in any order;
+    #     ragged edges (M, K not multiples of 8) and an all-zero band
+    for name, (M, K, p) in {"64x64": (64, 64, 0.1), "37x91": (37, 91, 0.2),
+                            "200x130": (200, 130, 0.03)}.items():
+        A = rng.random((M, K)) < p
+        A[8:16] = False
+        r, c = np.nonzero(A)
+        perm = rng.permutation(len(r))
+        bmp, tr, tc, ix, _ = R.coo2bmp(r[perm], c[perm], np.ones(len(r), np.float32), M, K)
+        fx["bmp_%s_words" % name] = W.pack_bits(A)
+        fx["bmp_%s_shape" % name] = np.array([M, K], np.int32)
+        fx["bmp_%s_bmp" % name] = bmp
+        fx["bmp_%s_tile_row" % name] = tr
+        fx["bmp_%s_tile_col" % name] = tc
+        fx["bmp_%s_idx" % name] = ix
+
+    # 11. the 1024x1024 Bernoulli(0.1) matrix of the small plain SpMM (seed 0):
+    #     the reference's packing (MSB-first) and row groups at its own
+    #     TILE_HEIGHT of 512 rows and MAX_GROUP_NUM of 2
+    c1 = W.config1()
+    A1 = W.unpack_bits(c1["words"], c1["K"]).astype(np.float32)
+    w1 = R.dense2bitmask(A1, 512)
+    g1 = R.generate_groups_large(w1, A1, 512)
+    fx["c1_words_msb"] = w1
+    fx["c1_group_id_ref"] = g1["group_id"]
+    fx["c1_group_mask_ref"] = g1["group_mask"]
+    fx["c1_group_nnz_ref"] = g1["nnz"]
+
     np.savez_compressed(OUT, **fx)
     print("wrote", OUT, {k: getattr(v, "shape", ()) for k, v in fx.items()})
 
