@@ -86,16 +86,20 @@ __global__ void __launch_bounds__(256) k_spmm_rows(SpmmArgs a) {
 // Prototype rows, register path: one warp per (clustered row, column chunk).
 // The delta gathers are issued first; P[c] is read after griddep_wait(), so
 // with programmatic dependent launch the whole gather phase overlaps the
-// prototype-sum kernel.  MINB caps registers (occupancy sweep).
-template <typename BT, int VPL, int D, int MINB>
+// prototype-sum kernel.  MINB caps registers (occupancy sweep).  OFF32 = B's
+// element offsets fit in 32 bits (K·ldb < 2^31) and FULL = every column
+// chunk is whole (N a multiple of the chunk width); with 32-bit row
+// arithmetic (M < 2^31, checked on the host) they keep the 8-blocks-per-SM
+// shape within its 32 registers without spilling (a 12-byte spill cost the
+// clustered 8192²×512 step 3 µs).
+template <typename BT, int VPL, int D, int MINB, bool OFF32, bool FULL>
 __global__ void __launch_bounds__(256, MINB) k_spmm_proto_regs(SpmmArgs a) {
   using V = Vec<BT>;
   constexpr int COLS = V::COLS;
   constexpr int CW = 32 * VPL * COLS;
   const int lane = threadIdx.x & 31;
-  const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const bool live = row < a.M;
-  const int cl = live ? __ldg(a.row_cluster + row) : -1;
+  const int row = (int)blockIdx.x * 8 + (threadIdx.x >> 5);
+  const int cl = row < (int)a.M ? __ldg(a.row_cluster + row) : -1;
   if (cl >= 0) {
     const int n0 = (int)blockIdx.y * CW;
     const BT* __restrict__ B = static_cast<const BT*>(a.B);
@@ -104,15 +108,16 @@ __global__ void __launch_bounds__(256, MINB) k_spmm_proto_regs(SpmmArgs a) {
 #pragma unroll
     for (int v = 0; v < VPL; v++) {
       col[v] = n0 + (v * 32 + lane) * COLS;
-      cvalid[v] = col[v] < a.N;
+      cvalid[v] = FULL || col[v] < (int)a.N;
     }
     ListWalker wk;
     wk.init(a.delta_idx, __ldg(a.delta_ptr + row), __ldg(a.delta_ptr + row + 1), lane);
     Acc<VPL, COLS, false> acc;
     acc.zero();
-    accumulate_walk<BT, VPL, D, false>(wk, B, a.ldb, col, cvalid, acc);
+    if (OFF32) accumulate_walk<BT, VPL, D, false>(wk, B, (uint32_t)a.ldb, col, cvalid, acc);
+    else accumulate_walk<BT, VPL, D, false>(wk, B, a.ldb, col, cvalid, acc);
     ptx::griddep_wait();
-    store_vecs<VPL, COLS, false>(a.C + row * a.ldc, col, cvalid, acc, a.P + (int64_t)cl * a.ldp);
+    store_vecs<VPL, COLS, false>(a.C + (int64_t)row * a.ldc, col, cvalid, acc, a.P + (int64_t)cl * a.ldp);
   } else {
     ptx::griddep_wait();
   }
@@ -225,7 +230,13 @@ int launch_proto_regs_t(const SpmmArgs& a, cudaStream_t s) {
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  BSP_CUDA(cudaLaunchKernelEx(&cfg, k_spmm_proto_regs<BT, VPL, D, MINB>, a));
+  const bool off32 = a.K * a.ldb < ((int64_t)1 << 31), full = a.N % CW == 0;
+  if (off32 && full)
+    BSP_CUDA(cudaLaunchKernelEx(&cfg, k_spmm_proto_regs<BT, VPL, D, MINB, true, true>, a));
+  else if (off32)
+    BSP_CUDA(cudaLaunchKernelEx(&cfg, k_spmm_proto_regs<BT, VPL, D, MINB, true, false>, a));
+  else
+    BSP_CUDA(cudaLaunchKernelEx(&cfg, k_spmm_proto_regs<BT, VPL, D, MINB, false, false>, a));
   return BSP_OK;
 }
 

@@ -142,8 +142,8 @@ struct Acc {
 
 // Gathers D rows of B at a time (this lane's VPL vectors of each) and adds
 // them in stream order; entries with bit 31 set are subtracted.
-template <typename BT, int VPL, int D, bool COMP, typename Walker>
-__device__ __forceinline__ void accumulate_walk(Walker& wk, const BT* __restrict__ B, int64_t ldb,
+template <typename BT, int VPL, int D, bool COMP, typename Walker, typename LD = int64_t>
+__device__ __forceinline__ void accumulate_walk(Walker& wk, const BT* __restrict__ B, LD ldb,
                                                 const int* col, const bool* cvalid,
                                                 Acc<VPL, Vec<BT>::COLS, COMP>& acc) {
   using V = Vec<BT>;
@@ -155,7 +155,7 @@ __device__ __forceinline__ void accumulate_walk(Walker& wk, const BT* __restrict
     typename V::Raw raw[D][VPL];
 #pragma unroll
     for (int s = 0; s < D; s++) {
-      const BT* brow = B + (int64_t)(idx[s] & 0x7fffffffu) * ldb;
+      const BT* brow = B + (LD)(idx[s] & 0x7fffffffu) * ldb;
 #pragma unroll
       for (int v = 0; v < VPL; v++)
         if (idx[s] != kEnd && cvalid[v]) raw[s][v] = V::load(brow + col[v]);
