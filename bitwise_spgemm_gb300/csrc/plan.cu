@@ -422,7 +422,10 @@ __global__ void __launch_bounds__(kConsThreads) k_consensus(const uint32_t* __re
   if (threadIdx.x == 0) {
     unsigned long long total = 0;
     for (int i = 0; i < kConsThreads / 32; i++) total += wpop[i];
-    if (total) atomicAdd(stats + 4, total);
+    if (total) {
+      atomicAdd(stats + 4, total);
+      atomicMax(stats + 7, total);
+    }
   }
   const int j = threadIdx.x;
   if (j < H / 2) {
@@ -928,6 +931,7 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
   plan->proto_nnz = (int64_t)st[4];
   plan->occ_tiles = (int64_t)st[5];
   plan->occT_tiles = (int64_t)st[6];
+  plan->proto_max_nnz = (int64_t)st[7];
   if (plan->delta_nnz >= INT_MAX) return BSP_ERR_CAPACITY;
 
   // Cost model in gathered rows of B: direct = nnz; proto = prototype bits +

@@ -7,6 +7,7 @@ struct bsp_plan {
   int mode = BSP_PLAN_DIRECT;
   int device = 0;
   int64_t nnz = 0, n_proto = 0, proto_nnz = 0, delta_nnz = 0, direct_rows = 0, direct_nnz = 0;
+  int64_t proto_max_nnz = 0;  // set bits of the densest prototype (compensated sums above 4096)
   // device storage (owned)
   void* arena = nullptr;        // row_cluster, delta_ptr, cons
   void* delta_arena = nullptr;  // delta_idx

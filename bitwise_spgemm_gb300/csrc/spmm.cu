@@ -154,13 +154,15 @@ __global__ void __launch_bounds__(256) k_spmm_rows_scalar(SpmmArgs a) {
 
 // P[c][n0 .. n0+32*COLS) for one prototype per CTA row: warp w walks the
 // prototype's words [w*Kw/W, (w+1)*Kw/W), partial sums meet in shared memory
-// and are added in warp order.
-template <typename BT, int D>
+// and are added in warp order.  COMP (the densest prototype has more than
+// 4096 set bits): each warp keeps a TwoSum pair (sum, error) and the pairs
+// are added with TwoSum too; P = sum + error.
+template <typename BT, int D, bool COMP, bool OFF32>
 __global__ void __launch_bounds__(512) k_proto_sums(SpmmArgs a) {
   using V = Vec<BT>;
   constexpr int COLS = V::COLS;
   constexpr int CW = 32 * COLS;
-  extern __shared__ float part[];  // [W][CW]
+  extern __shared__ float part[];  // [W][CW] sums, then (COMP) [W][CW] errors
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, W = blockDim.x >> 5;
   const int64_t c = blockIdx.x;
   const int64_t n0 = (int64_t)blockIdx.y * CW;
@@ -172,16 +174,29 @@ __global__ void __launch_bounds__(512) k_proto_sums(SpmmArgs a) {
   const int w0 = (int)(a.Kw * wid / W), w1 = (int)(a.Kw * (wid + 1) / W);
   BitWalker wk;
   wk.init(cw, w0, w1, lane);
-  Acc<1, COLS, false> acc;
+  Acc<1, COLS, COMP> acc;
   acc.zero();
-  accumulate_walk<BT, 1, D, false>(wk, B, a.ldb, col, cvalid, acc);
+  if (OFF32) accumulate_walk<BT, 1, D, COMP>(wk, B, (uint32_t)a.ldb, col, cvalid, acc);
+  else accumulate_walk<BT, 1, D, COMP>(wk, B, a.ldb, col, cvalid, acc);
 #pragma unroll
-  for (int j = 0; j < COLS; j++) part[wid * CW + lane * COLS + j] = acc.result(0, j);
+  for (int j = 0; j < COLS; j++) {
+    part[wid * CW + lane * COLS + j] = acc.s[0][j];
+    if (COMP) part[(W + wid) * CW + lane * COLS + j] = acc.c[0][COMP ? j : 0];
+  }
   __syncthreads();
   for (int j = threadIdx.x; j < CW; j += blockDim.x) {
-    float s = 0.f;
-    for (int w = 0; w < W; w++) s += part[w * CW + j];
-    if (n0 + j < a.N) a.P[c * a.ldp + n0 + j] = s;
+    float s = 0.f, e = 0.f;
+    for (int w = 0; w < W; w++) {
+      const float x = part[w * CW + j];
+      if (COMP) {
+        const float t = s + x, bp = t - s;
+        e += ((s - (t - bp)) + (x - bp)) + part[(W + w) * CW + j];
+        s = t;
+      } else {
+        s += x;
+      }
+    }
+    if (n0 + j < a.N) a.P[c * a.ldp + n0 + j] = COMP ? s + e : s;
   }
 }
 
@@ -260,9 +275,14 @@ template <typename BT>
 int launch_proto_t(const SpmmArgs& a, cudaStream_t s) {
   constexpr int CW = 32 * Vec<BT>::COLS;
   const int threads = 512;
-  const size_t smem = (size_t)(threads / 32) * CW * sizeof(float);
+  const bool comp = a.proto_max_nnz > kCompThreshold;
+  const size_t smem = (size_t)(threads / 32) * CW * sizeof(float) * (comp ? 2 : 1);
   const dim3 g((unsigned)a.n_proto, (unsigned)ceil_div(a.N, CW));
-  k_proto_sums<BT, 8><<<g, threads, smem, s>>>(a);
+  const bool off32 = a.K * a.ldb < ((int64_t)1 << 31);
+  if (comp && off32) k_proto_sums<BT, 8, true, true><<<g, threads, smem, s>>>(a);
+  else if (comp) k_proto_sums<BT, 8, true, false><<<g, threads, smem, s>>>(a);
+  else if (off32) k_proto_sums<BT, 8, false, true><<<g, threads, smem, s>>>(a);
+  else k_proto_sums<BT, 8, false, false><<<g, threads, smem, s>>>(a);
   BSP_LAUNCHED();
   return BSP_OK;
 }

@@ -37,6 +37,7 @@ struct SpmmArgs {
   int64_t n_delta;             // entries in delta_idx
   const uint32_t* cons;        // [n_proto][Kw] prototype masks
   int64_t n_proto;
+  int64_t proto_max_nnz;       // set bits of the densest prototype (TwoSum above 4096)
   float* P;                    // [n_proto][ldp] prototype sums (workspace)
   int64_t ldp;
   // optional row subset for the walking kernel (rows of A without a cluster)

@@ -140,6 +140,29 @@ def test_heavy_rows_compensated():
     assert np.abs(C - C64).max() < 0.5 * np.abs(C32 - C64).max()
 
 
+def test_dense_prototypes_compensated():
+    """Prototypes with more than 4096 set bits: their sums P[c] are formed
+    with TwoSum pairs, so clustered rows stay as close to FP64 as the
+    compensated direct walk, and integer-valued B stays exact."""
+    rng = np.random.default_rng(11)
+    M, K, N = 256, 16384, 256
+    A, _, _ = W.clustered_bits(M, K, n_proto=4, p_proto=0.4, p_flip=0.002, seed_proto=12, seed_rows=13)
+    words = W.pack_bits(A)
+    wd = words_dev(words)
+    plan = ops.Plan(wd, K, mode=capi.PLAN_PROTO)
+    assert plan.info()["mode"] == capi.PLAN_PROTO and plan.info()["n_proto"] >= 1
+    Bf = (rng.standard_normal((K, N)) * 1e3 + 1.0).astype(np.float32)
+    C = ops.spmm(wd, K, torch.from_numpy(Bf).cuda(), plan=plan).cpu().numpy()
+    assert capi.device_status() == 0
+    _check_f64(C, words, K, Bf)
+    C64 = O.spmm_f64(words, K, Bf)
+    C32 = O.spmm_f32(words, K, Bf)
+    assert np.abs(C - C64).max() < 0.5 * np.abs(C32 - C64).max()
+    Bi = rng.integers(-8, 9, (K, N)).astype(np.float32)
+    Ci = ops.spmm(wd, K, torch.from_numpy(Bi).cuda(), plan=plan).cpu().numpy()
+    assert np.array_equal(Ci.astype(np.float64), O.spmm_f64(words, K, Bi))
+
+
 def test_empty_and_degenerate():
     wd = torch.zeros((0, 2), dtype=torch.int32, device="cuda")
     B = torch.randn(40, 8, device="cuda")
