@@ -49,6 +49,12 @@ class Problem(C.Structure):
                 ("ldb", C.c_int64), ("C", C.c_void_p), ("ldc", C.c_int64)]
 
 
+class ProblemGrad(C.Structure):
+    _fields_ = [("A_words", C.c_void_p), ("M", C.c_int64), ("K", C.c_int64), ("X", C.c_void_p),
+                ("ldx", C.c_int64), ("G", C.c_void_p), ("ldg", C.c_int64), ("dX", C.c_void_p),
+                ("lddx", C.c_int64), ("dA", C.c_void_p), ("ldda", C.c_int64)]
+
+
 _P = C.c_void_p
 _I64 = C.c_int64
 _I = C.c_int
@@ -77,6 +83,8 @@ SIGNATURES = {
     "bsp_batch_create": [C.POINTER(Problem), _I, _I64, _I, C.POINTER(_P), _P],
     "bsp_batch_destroy": [_P],
     "bsp_batched_spmm": [_P, _P],
+    "bsp_batch_grad_create": [C.POINTER(ProblemGrad), _I, _I64, _I, C.POINTER(_P), _P],
+    "bsp_batched_spmm_grad": [_P, _P],
     "bsp_spmm_t": [_P, _I64, _I64, _P, _I, _I64, _I64, _P, _I64, _P, _P, _SZ, _P],
     "bsp_sddmm": [_P, _I64, _I64, _P, _I64, _P, _I64, _I, _I64, _P, _I64, _P, _P],
     "bsp_symbolic_rows": [_P, _I64, _I64, _P, _I64, _P, _P],

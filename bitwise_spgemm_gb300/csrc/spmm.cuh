@@ -10,17 +10,24 @@ namespace bsp {
 // boxes, 128-byte swizzle; first, so the record keeps the map's alignment), A
 // and C.
 struct BatchProblemTc {
-  CUtensorMap map;
+  CUtensorMap map;   // forward: B [K][N]; Aᵀ·G: G [M][N] (64x32 boxes); SDDMM: G [M][N] (64x256 boxes)
+  CUtensorMap map2;  // SDDMM: X [K][N] (64x256 boxes); otherwise unused
   const uint32_t* A;
   int64_t M, K, Kw;
-  float* C;
+  float* C;          // forward: C [M][N]; Aᵀ·G: dX [K][N]; SDDMM: dA [M][K]
   int64_t ldc;
 };
-// Tensor map of a batch problem's B [K][N] (row stride ldb elements).
+// Tensor map of a batch problem's B [K][N] (row stride ldb elements), or of
+// G [M][N] for the batched Aᵀ·G: 64-column x 32-row boxes.
 int make_batch_map(CUtensorMap* m, const void* B, int bdt, int64_t K, int64_t N, int64_t ldb);
-// Work item b = {problem, 256-row block, 256-column block, K tiles}: one CTA each.
+// Tensor map of G [M][N] or X [K][N] for the batched SDDMM: 64-column x
+// 256-row boxes.
+int make_batch_map_sddmm(CUtensorMap* m, const void* T, int bdt, int64_t rows, int64_t N, int64_t ld);
+// Work item b = {problem, 256-row block, 256-column block, reduction tiles}:
+// one CTA each.  kind 0 = forward C = A·B, 1 = dX = Aᵀ·G (rows: K),
+// 2 = dA = (G·Xᵀ) ⊙ A (columns: K).
 int launch_batched_tc(const BatchProblemTc* probs, const int4* items, int n_items, int64_t N, int bdt,
-                      cudaStream_t s);
+                      cudaStream_t s, int kind = 0);
 
 struct SpmmArgs {
   const uint32_t* A;  // packed rows [M][Kw], LSB-first

@@ -398,13 +398,60 @@ struct bsp_batch {
   int n = 0;
   int64_t N = 0;
   int bdt = BSP_BF16;
-  int n_items = 0;
+  int grad = 0;         // 0: forward batch (bsp_batch_create), 1: gradient batch (bsp_batch_grad_create)
+  int n_items = 0;      // forward items, or the Aᵀ·G items of a gradient batch
+  int n_items_s = 0;    // SDDMM items of a gradient batch
   int device = 0;
-  void* dev = nullptr;  // BatchProblemTc[n], int4 items[n_items], the work-queue counter
-  bsp::BatchProblemTc* probs = nullptr;
+  void* dev = nullptr;  // records, items, the work-queue counter
+  bsp::BatchProblemTc* probs = nullptr;    // forward, or Aᵀ·G (map = G)
+  bsp::BatchProblemTc* probs_s = nullptr;  // SDDMM (map = G, map2 = X)
   int4* items = nullptr;
+  int4* items_s = nullptr;
   int* counter = nullptr;  // next item of the persistent kernel (reset by every run)
 };
+
+namespace {
+
+// Uploads records and items into one device block and fills the batch.
+int batch_upload(bsp_batch* b, const std::vector<bsp::BatchProblemTc>& p1, const std::vector<int4>& i1,
+                 const std::vector<bsp::BatchProblemTc>& p2, const std::vector<int4>& i2, cudaStream_t s) {
+  using namespace bsp;
+  auto up = [](size_t bytes) { return (std::max<size_t>(bytes, 1) + 255) & ~size_t(255); };
+  const size_t o_p1 = 0, o_i1 = o_p1 + up(sizeof(BatchProblemTc) * p1.size());
+  const size_t o_p2 = o_i1 + up(sizeof(int4) * i1.size()), o_i2 = o_p2 + up(sizeof(BatchProblemTc) * p2.size());
+  const size_t o_c = o_i2 + up(sizeof(int4) * i2.size()), total = o_c + 256;
+  cudaError_t e = cudaMalloc(&b->dev, total);
+  if (e != cudaSuccess) {
+    cuda_status(e);
+    b->dev = nullptr;
+    return BSP_ERR_ALLOC;
+  }
+  char* base = static_cast<char*>(b->dev);
+  b->probs = reinterpret_cast<BatchProblemTc*>(base + o_p1);
+  b->items = reinterpret_cast<int4*>(base + o_i1);
+  b->probs_s = reinterpret_cast<BatchProblemTc*>(base + o_p2);
+  b->items_s = reinterpret_cast<int4*>(base + o_i2);
+  b->counter = reinterpret_cast<int*>(base + o_c);
+  b->n_items = (int)i1.size();
+  b->n_items_s = (int)i2.size();
+  struct Part { void* dst; const void* src; size_t bytes; };
+  const Part parts[4] = {{b->probs, p1.data(), sizeof(BatchProblemTc) * p1.size()},
+                         {b->items, i1.data(), sizeof(int4) * i1.size()},
+                         {b->probs_s, p2.data(), sizeof(BatchProblemTc) * p2.size()},
+                         {b->items_s, i2.data(), sizeof(int4) * i2.size()}};
+  for (const Part& q : parts)
+    if (q.bytes && (e = cudaMemcpyAsync(q.dst, q.src, q.bytes, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+      return cuda_status(e);
+  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_status(e);
+  return BSP_OK;
+}
+
+// longest reduction first (LPT), ties by problem order: stable
+void sort_items(std::vector<int4>& items) {
+  std::stable_sort(items.begin(), items.end(), [](const int4& x, const int4& y) { return x.w > y.w; });
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -431,7 +478,7 @@ int bsp_batch_create(const bsp_problem* problems, int n, int64_t N, int b_dtype,
       return BSP_ERR_ALIGNMENT;
     const int64_t Kw = ceil_div(p.K, 32);
     BatchProblemTc& r = hp[(size_t)i];
-    std::memset(&r.map, 0, sizeof(r.map));
+    std::memset(&r, 0, sizeof(r));
     if (p.K > 0 && N > 0) BSP_TRY(make_batch_map(&r.map, p.B, b_dtype, p.K, N, p.ldb));
     r.A = p.A_words;
     r.M = p.M;
@@ -443,39 +490,99 @@ int bsp_batch_create(const bsp_problem* problems, int n, int64_t N, int b_dtype,
       for (int64_t nb = 0; nb < ceil_div(N, kItemCols); nb++) items.push_back(make_int4(i, (int)rb, (int)nb, (int)Kw));
   }
   if (items.size() > (size_t)INT32_MAX) return BSP_ERR_CAPACITY;
-  // longest reduction first (LPT), ties by problem order: stable
-  std::stable_sort(items.begin(), items.end(), [](const int4& x, const int4& y) { return x.w > y.w; });
+  sort_items(items);
   bsp_batch* b = new (std::nothrow) bsp_batch();
   if (!b) return BSP_ERR_ALLOC;
   b->n = n;
   b->N = N;
   b->bdt = b_dtype;
-  b->n_items = (int)items.size();
   cudaGetDevice(&b->device);
-  const size_t pbytes = sizeof(BatchProblemTc) * (size_t)std::max(n, 1);
-  const size_t ibytes = sizeof(int4) * std::max<size_t>(items.size(), 1);
-  const size_t poff = (pbytes + 255) & ~size_t(255);
-  const size_t coff = poff + ((ibytes + 255) & ~size_t(255));
-  cudaError_t e = cudaMalloc(&b->dev, coff + 256);
-  if (e != cudaSuccess) {
-    cuda_status(e);
-    delete b;
-    return BSP_ERR_ALLOC;
-  }
-  b->probs = static_cast<BatchProblemTc*>(b->dev);
-  b->items = reinterpret_cast<int4*>(static_cast<char*>(b->dev) + poff);
-  b->counter = reinterpret_cast<int*>(static_cast<char*>(b->dev) + coff);
-  const cudaStream_t s = (cudaStream_t)stream;
-  int st = BSP_OK;
-  if (n > 0 &&
-      (e = cudaMemcpyAsync(b->probs, hp.data(), sizeof(BatchProblemTc) * n, cudaMemcpyHostToDevice, s)) != cudaSuccess)
-    st = cuda_status(e);
-  if (st == BSP_OK && !items.empty() &&
-      (e = cudaMemcpyAsync(b->items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice, s)) != cudaSuccess)
-    st = cuda_status(e);
-  if (st == BSP_OK && (e = cudaStreamSynchronize(s)) != cudaSuccess) st = cuda_status(e);
+  const int st = batch_upload(b, hp, items, {}, {}, (cudaStream_t)stream);
   if (st != BSP_OK) {
-    cudaFree(b->dev);
+    if (b->dev) cudaFree(b->dev);
+    delete b;
+    return st;
+  }
+  *batch = b;
+  return BSP_OK;
+}
+
+int bsp_batch_grad_create(const bsp_problem_grad* problems, int n, int64_t N, int dtype, bsp_batch** batch,
+                          bsp_stream_t stream) {
+  using namespace bsp;
+  if (!batch) return BSP_ERR_INVALID_ARG;
+  *batch = nullptr;
+  if (n < 0 || N < 0 || N > ((int64_t)1 << 30)) return BSP_ERR_INVALID_ARG;
+  if (n > 0 && !problems) return BSP_ERR_INVALID_ARG;
+  if (dtype != BSP_BF16 && dtype != BSP_F16) return BSP_ERR_UNSUPPORTED;
+  if (N % 8 != 0) return BSP_ERR_ALIGNMENT;
+  std::vector<BatchProblemTc> pt, ps;
+  std::vector<int4> it, is;
+  for (int i = 0; i < n; i++) {
+    const bsp_problem_grad& p = problems[i];
+    if (p.M < 0 || p.K < 0 || p.M > INT32_MAX || p.K > INT32_MAX) return BSP_ERR_INVALID_ARG;
+    if (p.ldx < N || p.ldg < N) return BSP_ERR_INVALID_ARG;
+    if (p.dX && p.lddx < N) return BSP_ERR_INVALID_ARG;
+    if (p.dA && p.ldda < p.K) return BSP_ERR_INVALID_ARG;
+    const bool work = p.M > 0 && p.K > 0;
+    if (work && (!p.A_words || (N > 0 && (!p.X || !p.G)))) return BSP_ERR_INVALID_ARG;
+    if (!is_aligned(p.A_words, 4) || !is_aligned(p.X, 16) || !is_aligned(p.G, 16) || (p.ldx * 2) % 16 != 0 ||
+        (p.ldg * 2) % 16 != 0)
+      return BSP_ERR_ALIGNMENT;
+    const int64_t Kw = ceil_div(p.K, 32);
+    if (p.dX && p.K > 0) {  // dX = Aᵀ·G: output rows K, reduction over M in 32-row tiles
+      if (ceil_div(p.M, 32) * 32 > tc_max_reduction()) return BSP_ERR_CAPACITY;
+      if (!is_aligned(p.dX, 16) || p.lddx % 4 != 0) return BSP_ERR_ALIGNMENT;
+      BatchProblemTc r;
+      std::memset(&r, 0, sizeof(r));
+      if (p.M > 0 && N > 0) BSP_TRY(make_batch_map(&r.map, p.G, dtype, p.M, N, p.ldg));
+      r.A = p.A_words;
+      r.M = p.M;
+      r.K = p.K;
+      r.Kw = Kw;
+      r.C = p.dX;
+      r.ldc = p.lddx;
+      const int idx = (int)pt.size();
+      pt.push_back(r);
+      for (int64_t rb = 0; rb < ceil_div(p.K, kItemRows); rb++)
+        for (int64_t nb = 0; nb < ceil_div(N, kItemCols); nb++)
+          it.push_back(make_int4(idx, (int)rb, (int)nb, (int)ceil_div(p.M, 32)));
+    }
+    if (p.dA && p.M > 0) {  // dA = (G·Xᵀ) ⊙ A: output [M][K], reduction over N in 64-column steps
+      if (p.K % 8 != 0 || !is_aligned(p.dA, 16) || p.ldda % 4 != 0) return BSP_ERR_ALIGNMENT;
+      if (ceil_div(p.K, kItemCols) > INT32_MAX) return BSP_ERR_CAPACITY;
+      BatchProblemTc r;
+      std::memset(&r, 0, sizeof(r));
+      if (p.K > 0 && N > 0) {
+        BSP_TRY(make_batch_map_sddmm(&r.map, p.G, dtype, p.M, N, p.ldg));
+        BSP_TRY(make_batch_map_sddmm(&r.map2, p.X, dtype, p.K, N, p.ldx));
+      }
+      r.A = p.A_words;
+      r.M = p.M;
+      r.K = p.K;
+      r.Kw = Kw;
+      r.C = p.dA;
+      r.ldc = p.ldda;
+      const int idx = (int)ps.size();
+      ps.push_back(r);
+      for (int64_t rb = 0; rb < ceil_div(p.M, kItemRows); rb++)
+        for (int64_t kb = 0; kb < ceil_div(p.K, kItemCols); kb++)
+          is.push_back(make_int4(idx, (int)rb, (int)kb, (int)ceil_div(N, 64)));
+    }
+  }
+  if (it.size() > (size_t)INT32_MAX || is.size() > (size_t)INT32_MAX) return BSP_ERR_CAPACITY;
+  sort_items(it);
+  sort_items(is);
+  bsp_batch* b = new (std::nothrow) bsp_batch();
+  if (!b) return BSP_ERR_ALLOC;
+  b->n = n;
+  b->N = N;
+  b->bdt = dtype;
+  b->grad = 1;
+  cudaGetDevice(&b->device);
+  const int st = batch_upload(b, pt, it, ps, is, (cudaStream_t)stream);
+  if (st != BSP_OK) {
+    if (b->dev) cudaFree(b->dev);
     delete b;
     return st;
   }
@@ -492,7 +599,7 @@ int bsp_batch_destroy(bsp_batch* batch) {
 
 int bsp_batched_spmm(const bsp_batch* b, bsp_stream_t stream) {
   using namespace bsp;
-  if (!b) return BSP_ERR_INVALID_ARG;
+  if (!b || b->grad) return BSP_ERR_INVALID_ARG;
   int dev = -1;
   cudaGetDevice(&dev);
   if (dev != b->device) return BSP_ERR_INVALID_ARG;
@@ -507,6 +614,18 @@ int bsp_batched_spmm(const bsp_batch* b, bsp_stream_t stream) {
     return BSP_ERR_UNSUPPORTED;
   }
   return launch_batched_tc(b->probs, b->items, b->n_items, b->N, b->bdt, s);
+}
+
+int bsp_batched_spmm_grad(const bsp_batch* b, bsp_stream_t stream) {
+  using namespace bsp;
+  if (!b || !b->grad) return BSP_ERR_INVALID_ARG;
+  int dev = -1;
+  cudaGetDevice(&dev);
+  if (dev != b->device) return BSP_ERR_INVALID_ARG;
+  if (b->N == 0) return BSP_OK;
+  const cudaStream_t s = (cudaStream_t)stream;
+  BSP_TRY(launch_batched_tc(b->probs, b->items, b->n_items, b->N, b->bdt, s, 1));
+  return launch_batched_tc(b->probs_s, b->items_s, b->n_items_s, b->N, b->bdt, s, 2);
 }
 
 }  // extern "C"

@@ -79,7 +79,12 @@ constexpr int kEpiWarps = 16;  // 4 TMEM lane quarters x 2 accumulators x 2 colu
 using tc::kLbo;
 using tc::kSbo;
 using tc::kLayoutSw128;
-constexpr int kFwd = 0, kTrans = 1, kSddmm = 2, kBatch = 3;
+constexpr int kFwd = 0, kTrans = 1, kSddmm = 2, kBatch = 3, kBatchT = 4, kBatchS = 5;
+// kBatch / kBatchT / kBatchS: the forward product, Aᵀ·G and the SDDMM of a
+// batch, CTA b running work item b with its problem's record
+__host__ __device__ constexpr bool batched_mode(int m) { return m == kBatch || m == kBatchT || m == kBatchS; }
+__host__ __device__ constexpr bool trans_mode(int m) { return m == kTrans || m == kBatchT; }
+__host__ __device__ constexpr bool sddmm_mode(int m) { return m == kSddmm || m == kBatchS; }
 // B (fwd) / G (trans) tile: four TMA boxes of 64 columns x 32 reduction rows,
 // 128-byte swizzle, kBox bytes apart (the LBO); 8-row groups 1 KB apart (SBO).
 constexpr int kBoxCols = 64;
@@ -150,7 +155,8 @@ template <typename BT, int MODE, int TPS>
 __global__ void __launch_bounds__(tc_threads(TPS), 1) k_spmm_tc(TcArgs a, const __grid_constant__ CUtensorMap mapA,
                                                                const __grid_constant__ CUtensorMap mapB) {
   constexpr int kTilesPerStage = TPS;
-  constexpr int kStageBytes = MODE == kSddmm ? kSdTile : TPS * kATile;
+  constexpr bool kSd = sddmm_mode(MODE), kTr = trans_mode(MODE), kBat = batched_mode(MODE);
+  constexpr int kStageBytes = kSd ? kSdTile : TPS * kATile;
   constexpr int kStages = kRingBytes / kStageBytes;
   constexpr int kProducerWarps = kGroupThreads * TPS / 32;
   constexpr int kTmaWarp = kProducerWarps;
@@ -167,9 +173,10 @@ __global__ void __launch_bounds__(tc_threads(TPS), 1) k_spmm_tc(TcArgs a, const 
   int64_t gM = a.M, gK = a.K, gKw = a.Kw, gldc = a.ldc;
   float* gC = a.C;
   const void* bmap = &mapB;
-  int64_t row0 = (int64_t)blockIdx.x * kCtaM;  // output rows: M (fwd, sddmm, batch) or K (trans)
-  int64_t col0 = (int64_t)blockIdx.y * kTcN;   // output columns: N (fwd, trans, batch) or K (sddmm)
-  if (MODE == kBatch) {
+  const void* amap = &mapA;
+  int64_t row0 = (int64_t)blockIdx.x * kCtaM;  // output rows: M (fwd, sddmm) or K (trans)
+  int64_t col0 = (int64_t)blockIdx.y * kTcN;   // output columns: N (fwd, trans) or K (sddmm)
+  if (kBat) {
     const int4 it = a.items[blockIdx.x];
     const BatchProblemTc& p = a.bprobs[it.x];
     gA = p.A;
@@ -178,22 +185,23 @@ __global__ void __launch_bounds__(tc_threads(TPS), 1) k_spmm_tc(TcArgs a, const 
     gKw = p.Kw;
     gC = p.C;
     gldc = p.ldc;
-    bmap = &p.map;
+    bmap = kSd ? &p.map2 : &p.map;  // SDDMM: X [K][N] (the B side), G [M][N] (the A side)
+    amap = &p.map;
     row0 = (int64_t)it.y * kCtaM;
     col0 = (int64_t)it.z * kTcN;
   }
-  const int64_t out_rows = MODE == kTrans ? gK : gM;
-  const int64_t out_cols = MODE == kSddmm ? gK : a.N;
+  const int64_t out_rows = kTr ? gK : gM;
+  const int64_t out_cols = kSd ? gK : a.N;
   // B boxes (64 columns) holding output columns of this CTA: a narrow last
   // column tile loads, multiplies and stores only those (MMA N = 64·nbox)
-  const int nbox = MODE == kSddmm ? kTcN / kBoxCols
+  const int nbox = kSd ? kTcN / kBoxCols
                                   : (int)min((int64_t)(kTcN / kBoxCols), (out_cols - col0 + kBoxCols - 1) / kBoxCols);
   const int dense_halves = row0 + kTcM < out_rows ? 3 : 1;
 
   if (tid == 0) {
     for (int s = 0; s < kStages; s++) {
       // one arrival per producer warp + the TMA warp's (SDDMM: TMA only)
-      ptx::mbar_init(&sm.full[s], MODE == kSddmm ? 1 : kProducerWarps + 1);
+      ptx::mbar_init(&sm.full[s], kSd ? 1 : kProducerWarps + 1);
       ptx::mbar_init(&sm.empty[s], 1);
     }
     ptx::mbar_init(&sm.done, 1);
@@ -204,9 +212,11 @@ __global__ void __launch_bounds__(tc_threads(TPS), 1) k_spmm_tc(TcArgs a, const 
     ptx::tmem_alloc(&sm.tmem_addr, kTmemCols);
     ptx::tmem_relinquish();
   }
-  if (MODE == kBatch && warp == 0) {
-    // every K tile (a batch has no occupancy plan), both halves that hold rows
-    const int ntot = (int)min(gKw, (int64_t)kListMax);
+  if ((MODE == kBatch || MODE == kBatchT) && warp == 0) {
+    // every reduction tile (a batch has no occupancy plan): K tiles of the
+    // forward product, 32-row tiles of A for Aᵀ·G; both halves that hold rows
+    const int64_t red = MODE == kBatch ? gKw : (gM + kTcK - 1) / kTcK;
+    const int ntot = (int)min(red, (int64_t)kListMax);
     for (int k = lane; k < ntot; k += 32) sm.list[k] = k | (dense_halves << 28);
     __syncwarp();
     if (lane == 0) {
@@ -261,7 +271,7 @@ __global__ void __launch_bounds__(tc_threads(TPS), 1) k_spmm_tc(TcArgs a, const 
     }
   }
   // SDDMM: a block of A without set bits needs no product at all
-  if (MODE == kSddmm) {
+  if (kSd) {
     uint32_t acc = 0;
     if (tid < kCtaM && row0 + tid < gM) {
       const uint32_t* arow = gA + (row0 + tid) * gKw;
@@ -281,7 +291,7 @@ __global__ void __launch_bounds__(tc_threads(TPS), 1) k_spmm_tc(TcArgs a, const 
   const int n = sm.nlist;
   const int* lst = sm.list + sm.lo;  // this CTA's occupied tiles (fwd / trans)
   // stage i: list entries 2i and 2i+1 (fwd / trans) or N columns [64i, 64i+64) (SDDMM)
-  const int nstages = MODE == kSddmm ? n : (n + kTilesPerStage - 1) / kTilesPerStage;
+  const int nstages = kSd ? n : (n + kTilesPerStage - 1) / kTilesPerStage;
 
   if (warp < kProducerWarps) {
     // ---------------- A producers (fwd / trans) ----------------
@@ -289,7 +299,7 @@ __global__ void __launch_bounds__(tc_threads(TPS), 1) k_spmm_tc(TcArgs a, const 
     // or one (A row, word) pair (trans) per thread, from words loaded
     // kWordAhead stages ahead; each warp arrives once per stage after its
     // lanes' writes are fenced.  Lane 0 waits for the slot for the warp.
-    if (MODE != kSddmm) {
+    if (!kSd) {
       const int u = warp / (kGroupThreads / 32);
       const int r = tid % kGroupThreads;
       auto load_word = [&](int k) -> uint32_t {
@@ -298,12 +308,12 @@ __global__ void __launch_bounds__(tc_threads(TPS), 1) k_spmm_tc(TcArgs a, const 
         if (kFwdLike) {
           const int64_t arow = row0 + r;
           if (arow >= gM) return 0u;
-          return (MODE != kBatch && a.At) ? __ldg(a.At + (int64_t)t * gM + arow) : __ldg(gA + arow * gKw + t);
+          return (!kBat && a.At) ? __ldg(a.At + (int64_t)t * gM + arow) : __ldg(gA + arow * gKw + t);
         }
         const int64_t arow = (int64_t)t * kTcK + (r & 31);
         const int64_t wcol = row0 / 32 + (r >> 5);
         if (arow >= gM || wcol >= gKw) return 0u;
-        return a.At ? __ldg(a.At + wcol * gM + arow) : __ldg(gA + arow * gKw + wcol);
+        return (!kBat && a.At) ? __ldg(a.At + wcol * gM + arow) : __ldg(gA + arow * gKw + wcol);
       };
       uint32_t wq[kWordAhead];
 #pragma unroll
@@ -350,7 +360,10 @@ __global__ void __launch_bounds__(tc_threads(TPS), 1) k_spmm_tc(TcArgs a, const 
     // ---------------- TMA issuer ----------------
     // Shared-memory addresses are formed once; a stage adds its offset.
     const uint32_t a0 = ptx::smem_addr(sm.a), b0 = ptx::smem_addr(sm.b), f0 = ptx::smem_addr(&sm.full[0]);
-    if (MODE == kBatch) ptx::tensormap_acquire(bmap);  // written by the host into global memory
+    if (kBat) {  // written by the host into global memory
+      ptx::tensormap_acquire(bmap);
+      if (kSd) ptx::tensormap_acquire(amap);
+    }
     for (int i = 0; i < nstages; i++) {
       const int s = i % kStages;
       if (i >= kStages && !ptx::mbar_wait(&sm.empty[s], ((i / kStages) - 1) & 1)) {
@@ -359,17 +372,17 @@ __global__ void __launch_bounds__(tc_threads(TPS), 1) k_spmm_tc(TcArgs a, const 
         break;
       }
       const uint32_t fb = f0 + s * 8, as = a0 + s * kStageBytes, bs = b0 + s * kStageBytes;
-      if (MODE == kSddmm) {
+      if (kSd) {
         // G rows row0.. and X rows col0.. (256 each), N columns i*64..
         ptx::mbar_arrive_expect_tx(&sm.full[s], 2 * kSdTile);
-        ptx::tma_load_2d_u32(as, &mapA, i * kSdK, (int)row0, fb);
-        ptx::tma_load_2d_u32(bs, &mapB, i * kSdK, (int)col0, fb);
+        ptx::tma_load_2d_u32(as, amap, i * kSdK, (int)row0, fb);
+        ptx::tma_load_2d_u32(bs, bmap, i * kSdK, (int)col0, fb);
       } else {
         // B (fwd) / G (trans) rows t*32.. of the stage's tiles, columns col0 + 64*j
         const int k0 = kTilesPerStage * i;
         const int cnt = min(kTilesPerStage, n - k0);  // tiles in this stage
         ptx::mbar_arrive_expect_tx(&sm.full[s], cnt * nbox * kBox);
-        if (MODE != kBatch && a.bt) {
+        if (!kBat && a.bt) {
           // tiled B: each tile's first nbox atoms are one contiguous copy
 #pragma unroll
           for (int u = 0; u < kTilesPerStage; u++)
@@ -395,12 +408,12 @@ __global__ void __launch_bounds__(tc_threads(TPS), 1) k_spmm_tc(TcArgs a, const 
     // Descriptors of stage 0 are built once; every MMA adds a compile-time
     // offset (plus the stage's) to the 14-bit start-address field (>> 4).
     const uint32_t ab = std::is_same<BT, __nv_bfloat16>::value ? 1u : 0u;
-    const uint32_t idesc = tc::idesc_f16(ab, MODE == kTrans ? 1u : 0u, MODE == kSddmm ? 0u : 1u,
+    const uint32_t idesc = tc::idesc_f16(ab, kTr ? 1u : 0u, kSd ? 0u : 1u,
                                          (uint32_t)(nbox * kBoxCols), kTcM);
     const uint32_t a0 = ptx::smem_addr(sm.a), b0 = ptx::smem_addr(sm.b);
-    const uint64_t adesc = MODE == kSddmm ? ptx::smem_desc_noswizzle_u32(a0, 16, kSdSbo) | ((uint64_t)kLayoutSw128 << 61)
+    const uint64_t adesc = kSd ? ptx::smem_desc_noswizzle_u32(a0, 16, kSdSbo) | ((uint64_t)kLayoutSw128 << 61)
                                           : ptx::smem_desc_noswizzle_u32(a0, kLbo, kSbo);
-    const uint64_t bdesc = MODE == kSddmm ? ptx::smem_desc_noswizzle_u32(b0, 16, kSdSbo) | ((uint64_t)kLayoutSw128 << 61)
+    const uint64_t bdesc = kSd ? ptx::smem_desc_noswizzle_u32(b0, 16, kSdSbo) | ((uint64_t)kLayoutSw128 << 61)
                                           : ptx::smem_desc_noswizzle_u32(b0, kBox, 1024) | ((uint64_t)kLayoutSw128 << 61);
     // The tensor pipe queues about one MMA beyond the one it runs, so every
     // cycle this thread spends between stages is idle tensor time: the next
@@ -410,7 +423,7 @@ __global__ void __launch_bounds__(tc_threads(TPS), 1) k_spmm_tc(TcArgs a, const 
 #pragma unroll
       for (int u = 0; u < kTilesPerStage; u++) {
         const int k = kTilesPerStage * st + u;
-        hv[u] = MODE == kSddmm ? (u == 0 ? dense_halves : 0)
+        hv[u] = kSd ? (u == 0 ? dense_halves : 0)
                                : (st < nstages && k < n ? (lst[k] >> 28) & 3 : 0);
       }
     };
@@ -433,7 +446,7 @@ __global__ void __launch_bounds__(tc_threads(TPS), 1) k_spmm_tc(TcArgs a, const 
       ptx::tc_fence_after_sync();
       const uint64_t soff = (uint64_t)((s * kStageBytes) >> 4);
       const uint64_t as = adesc + soff, bs = bdesc + soff;
-      if (MODE == kSddmm) {
+      if (kSd) {
 #pragma unroll
         for (int h = 0; h < kHalves; h++) {
           if (!((hv0 >> h) & 1)) continue;
@@ -509,7 +522,7 @@ __global__ void __launch_bounds__(tc_threads(TPS), 1) k_spmm_tc(TcArgs a, const 
 #pragma unroll
           for (int v = 0; v < 8; v++) r[u][v] = 0u;
       }
-      if (MODE == kSddmm) {
+      if (kSd) {
         if (!live) continue;
         float* crow = cbase + row * cld + ccol;
 #pragma unroll
@@ -942,8 +955,12 @@ int make_batch_map(CUtensorMap* m, const void* B, int bdt, int64_t K, int64_t N,
   return make_map(m, B, bdt, K, N, ldb, kBoxCols, kTcK, CU_TENSOR_MAP_SWIZZLE_128B);
 }
 
+int make_batch_map_sddmm(CUtensorMap* m, const void* T, int bdt, int64_t rows, int64_t N, int64_t ld) {
+  return make_map(m, T, bdt, rows, N, ld, kSdK, kCtaM, CU_TENSOR_MAP_SWIZZLE_128B);
+}
+
 int launch_batched_tc(const BatchProblemTc* probs, const int4* items, int n_items, int64_t N, int bdt,
-                      cudaStream_t s) {
+                      cudaStream_t s, int kind) {
   if (n_items == 0 || N == 0) return BSP_OK;
   TcArgs a = {};
   a.N = N;
@@ -953,9 +970,17 @@ int launch_batched_tc(const BatchProblemTc* probs, const int4* items, int n_item
   CUtensorMap unused;
   memset(&unused, 0, sizeof(unused));
   const dim3 grid((unsigned)n_items, 1, 1);
-  if (bdt == BSP_BF16) return launch_mode<__nv_bfloat16, kBatch, 2>(a, unused, unused, grid, s);
-  if (bdt == BSP_F16) return launch_mode<__half, kBatch, 2>(a, unused, unused, grid, s);
-  return BSP_ERR_UNSUPPORTED;
+  if (bdt != BSP_BF16 && bdt != BSP_F16) return BSP_ERR_UNSUPPORTED;
+  const bool bf = bdt == BSP_BF16;
+  switch (kind) {
+    case 0: return bf ? launch_mode<__nv_bfloat16, kBatch, 2>(a, unused, unused, grid, s)
+                      : launch_mode<__half, kBatch, 2>(a, unused, unused, grid, s);
+    case 1: return bf ? launch_mode<__nv_bfloat16, kBatchT, 2>(a, unused, unused, grid, s)
+                      : launch_mode<__half, kBatchT, 2>(a, unused, unused, grid, s);
+    case 2: return bf ? launch_mode<__nv_bfloat16, kBatchS, 2>(a, unused, unused, grid, s)
+                      : launch_mode<__half, kBatchS, 2>(a, unused, unused, grid, s);
+    default: return BSP_ERR_INVALID_ARG;
+  }
 }
 
 int tc_device_error(int* out, bool clear) {

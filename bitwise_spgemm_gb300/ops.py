@@ -438,3 +438,43 @@ class Batch:
 
     def __del__(self):
         self.close()
+
+
+class BatchGrad:
+    """Backward pass of many Y_i = A_i·X_i (16-bit X and G, shared N) in two
+    tensor-core launches: dX_i = A_iᵀ·G_i and dA_i = (G_i·X_iᵀ) ⊙ A_i.
+    ``problems``: list of (words, K, X, G, dX, dA) tensors, dX or dA may be
+    None; the tensors are referenced by the batch and must outlive it.  Runs
+    of one batch must not overlap on the GPU (they write dX and dA)."""
+
+    def __init__(self, problems):
+        n = len(problems)
+        if n == 0:
+            raise ValueError("empty batch")
+        N = problems[0][2].shape[1]
+        dt = problems[0][2].dtype
+        arr = (capi.ProblemGrad * n)()
+        self._keep = []
+        ptr = lambda t: t.data_ptr() if t is not None and t.numel() else 0  # noqa: E731
+        for i, (words, K, X, G, dX, dA) in enumerate(problems):
+            if X.dtype != dt or G.dtype != dt or X.shape[1] != N or G.shape[1] != N:
+                raise ValueError("all problems of a batch share N and the X / G dtype")
+            arr[i] = capi.ProblemGrad(ptr(words), words.shape[0], K, ptr(X), _rowmajor(X, "X"), ptr(G),
+                                      _rowmajor(G, "G"), ptr(dX), _rowmajor(dX, "dX") if dX is not None else 0,
+                                      ptr(dA), _rowmajor(dA, "dA") if dA is not None else 0)
+            self._keep.append((words, X, G, dX, dA))
+        h = C.c_void_p()
+        call("bsp_batch_grad_create", arr, n, N, _DT[dt], C.byref(h), _stream())
+        self._h = h
+        self._lib = capi.lib()
+
+    def run(self):
+        call("bsp_batched_spmm_grad", self._h, _stream())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.bsp_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()

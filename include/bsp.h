@@ -269,6 +269,44 @@ int bsp_batch_destroy(bsp_batch* batch);
  * must not overlap on the GPU: they share the queue and the C buffers.     */
 int bsp_batched_spmm(const bsp_batch* batch, bsp_stream_t stream);
 
+/* One problem of a batched backward pass of Y = A·X (A a 0/1 mask, packed
+ * LSB-first words [M][ceil(K/32)]; X [K×N] and the incoming gradient
+ * G = dL/dY [M×N] 16-bit, row strides ldx, ldg elements, 16-byte aligned):
+ *   dX = Aᵀ·G            [K×N] FP32, row stride lddx (NULL: not computed)
+ *   dA = (G·Xᵀ) ⊙ A      [M×K] FP32, row stride ldda, zero off A's bits
+ *                         (the straight-through mask gradient; NULL: skip)
+ * dX and dA 16-byte aligned with strides a multiple of 4; dA needs
+ * K % 8 == 0.  Limit: M ≤ 131072 for dX (BSP_ERR_CAPACITY).               */
+typedef struct bsp_problem_grad {
+  const uint32_t* A_words;
+  int64_t M, K;
+  const void* X;
+  int64_t ldx;
+  const void* G;
+  int64_t ldg;
+  float* dX;
+  int64_t lddx;
+  float* dA;
+  int64_t ldda;
+} bsp_problem_grad;
+
+/* Prepare a gradient batch: n problems sharing N (multiple of 8) and the
+ * 16-bit type of X and G.  Encodes the G and X tensor maps, uploads them
+ * with two work lists — (problem, 256-row block of dX, 256-column block)
+ * and (problem, 256-row block of dA, 256-column block of dA) — sorted
+ * longest reduction first; synchronises the stream once.  Buffers are
+ * referenced and must outlive the batch; bsp_batch_destroy releases it.
+ * No reference counterpart (the reference has no backward pass); the
+ * single-problem forms are bsp_spmm_t and bsp_sddmm.                      */
+int bsp_batch_grad_create(const bsp_problem_grad* problems, int n, int64_t N,
+                          int dtype, bsp_batch** batch, bsp_stream_t stream);
+/* Every dX and dA of a gradient batch: two tensor-core launches (a CTA per
+ * work item), no host synchronisation, no allocation.  dX sums every 32-row
+ * tile of A (a batch has no occupancy plan); dA skips blocks of A without
+ * set bits and writes them as zeros.  Runs of one batch must not overlap
+ * on the GPU: they write the same dX and dA buffers.                       */
+int bsp_batched_spmm_grad(const bsp_batch* batch, bsp_stream_t stream);
+
 /* ======================================================================== */
 /* Autotuner                                                                */
 /* ======================================================================== */

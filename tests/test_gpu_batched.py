@@ -128,3 +128,73 @@ def test_persistent_matches_item_per_cta():
         assert r.returncode == 0, r.stderr[-2000:]
         outs.append(r.stdout.strip().splitlines()[-3:])
     assert outs[0] == outs[1]
+
+
+def _grad_problems(n, N, seed, integer):
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        M = int(32 * rng.integers(1, 48)) + (int(rng.integers(1, 31)) if i % 5 == 3 else 0)  # some ragged M
+        K = int(8 * rng.integers(4, 160))
+        d = float(rng.uniform(0.01, 0.3))
+        A = rng.random((M, K)) < d
+        if i == 2:
+            A[:, :] = False  # a problem without set bits: dX and dA are zero
+        draw = (lambda s: rng.integers(-4, 5, s)) if integer else (lambda s: rng.standard_normal(s))
+        X16 = W.f32_to_bf16_bits(draw((K, N)).astype(np.float32))
+        G16 = W.f32_to_bf16_bits(draw((M, N)).astype(np.float32))
+        out.append((A, W.pack_bits(A), K, X16, G16))
+    return out
+
+
+@pytest.mark.parametrize("N,integer", [(128, True), (128, False), (264, False)])
+def test_batched_grad_matches_oracle(N, integer):
+    """dX = Aᵀ·G and dA = (G·Xᵀ) ⊙ A for a batch of uneven problems against
+    the FP64 oracle (integer-valued X and G exactly, N(0,1) within the scaled
+    tolerance), against the single-problem bsp_spmm_t / bsp_sddmm, and
+    stable over two runs."""
+    probs = _grad_problems(20, N, seed=N + integer, integer=integer)
+    dev = []
+    for A, words, K, X16, G16 in probs:
+        M = words.shape[0]
+        wd = torch.from_numpy(np.ascontiguousarray(words).view(np.int32)).cuda()
+        dev.append((wd, K, bf16_dev(X16), bf16_dev(G16), torch.full((K, N), float("nan"), device="cuda"),
+                    torch.full((M, K), float("nan"), device="cuda")))
+    batch = ops.BatchGrad(dev)
+    for run in range(2):
+        batch.run()
+        torch.cuda.synchronize()
+        assert capi.device_status() == 0
+        for (A, words, K, X16, G16), (wd, _, Xd, Gd, dXd, dAd) in zip(probs, dev):
+            M = words.shape[0]
+            X, G = W.bf16_bits_to_f32(X16), W.bf16_bits_to_f32(G16)
+            dX, dA = dXd.cpu().numpy(), dAd.cpu().numpy()
+            dX64 = O.spmm_t_f64(words, M, K, G)
+            vals64 = O.sddmm_f64(words, M, K, G, X)
+            assert np.all(dA[~A] == 0.0)
+            if integer:
+                assert np.array_equal(dX.astype(np.float64), dX64)
+                assert np.array_equal(dA[A].astype(np.float64), vals64)
+            else:
+                mx, _, _ = O.rel_errors(dX, dX64, O.spmm_t_f64(words, M, K, np.abs(G)))
+                assert mx <= TOL
+                scale = (np.abs(G.astype(np.float64)) @ np.abs(X.astype(np.float64)).T)[A]
+                err = np.abs(dA[A] - vals64) / np.where(scale > 0, scale, 1.0)
+                assert err.size == 0 or err.max() <= TOL
+            if run == 0:
+                ref_dX = ops.spmm_t(wd, M, K, Gd).cpu().numpy()
+                ref_dA = ops.sddmm(wd, M, K, Gd, Xd).cpu().numpy()
+                assert np.abs(dX - ref_dX).max() <= 1e-3 * max(1.0, float(np.abs(ref_dX).max()))
+                assert np.abs(dA - ref_dA).max() <= 1e-3 * max(1.0, float(np.abs(ref_dA).max()))
+    batch.close()
+
+
+def test_batched_grad_validation():
+    w = torch.zeros((64, 2), dtype=torch.int32, device="cuda")
+    X = torch.zeros((60, 128), dtype=torch.bfloat16, device="cuda")
+    G = torch.zeros((64, 128), dtype=torch.bfloat16, device="cuda")
+    dA = torch.zeros((64, 60), device="cuda")
+    with pytest.raises(capi.BspError):  # dA needs K % 8 == 0
+        ops.BatchGrad([(w, 60, X, G, None, dA)])
+    fwd = ops.Batch([(w, 60, X, torch.zeros((64, 128), device="cuda"))])
+    assert capi.lib().bsp_batched_spmm_grad(fwd._h, None) == -1  # BSP_ERR_INVALID_ARG
