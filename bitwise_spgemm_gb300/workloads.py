@@ -132,6 +132,13 @@ def config4(n_problems=512, N=128):
     return [config4_problem(i, N) for i in range(n_problems)]
 
 
+def config4_grad(problem, i):
+    """Incoming gradient of problem i of the batched set for its backward
+    pass: G = dL/dY [M x N] N(0,1) bf16 (seed 100007+i)."""
+    G = np.random.default_rng(100007 + i).standard_normal((problem["M"], problem["N"]), dtype=np.float32)
+    return f32_to_bf16_bits(G)
+
+
 def config5(M=4096, K=4096, N=8192):
     """Mask A 4096x4096 Bernoulli(0.1) (seed 8); X, G 4096x8192 N(0,1) bf16
     (seeds 9, 10)."""
