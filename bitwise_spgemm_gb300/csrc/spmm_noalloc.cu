@@ -1,15 +1,18 @@
 // spmm_noalloc.cu — bsp_spmm_noalloc: the planned SpMM without a caller
 // workspace, for callers that may not allocate device memory when they run
-// the SpMM (plugin callbacks that are handed pointers only, code inside CUDA
-// stream capture, processes whose device memory belongs to another
-// allocator).
+// the SpMM (plugin callbacks that are handed pointers only, hot loops that
+// must not call the allocator, processes whose device memory belongs to
+// another allocator).
 //
-// The prototype sums that bsp_spmm keeps in the caller's workspace live
-// here in a file-scope device array of fixed size.  Its address is looked up
-// once per device with cudaGetSymbolAddress (a host-side name of a
-// __device__ array is not a device address), and the call then runs the
-// ordinary bsp_spmm path with that array as workspace.  No allocation
-// happens in this entry point.
+// The scratch that bsp_spmm keeps in the caller's workspace lives here in a
+// file-scope device array of fixed size: the prototype sums and, for 16-bit
+// B on the tensor cores, the split-K partials and the tiled copy of B where
+// they fit.  Its address is looked up once per device with
+// cudaGetSymbolAddress (a host-side name of a __device__ array is not a
+// device address), so the first call on a device must come before any
+// stream capture; the call then runs the ordinary bsp_spmm path with the
+// whole array as workspace, whatever the plan.  No allocation happens in
+// this entry point.
 #include <mutex>
 
 #include "bsp_internal.cuh"
@@ -53,7 +56,6 @@ extern "C" int bsp_spmm_noalloc(const uint32_t* A_words, int64_t M, int64_t K, c
   BSP_TRY(bsp_spmm_workspace(plan, N < 0 ? 0 : N, &need));
   if (need > bsp::kNoAllocBytes) return BSP_ERR_CAPACITY;
   void* scratch = nullptr;
-  if (need > 0) BSP_TRY(bsp::scratch_address(&scratch));
-  return bsp_spmm(A_words, M, K, B, b_dtype, ldb, N, C, ldc, plan, scratch, need ? bsp::kNoAllocBytes : 0,
-                  stream);
+  BSP_TRY(bsp::scratch_address(&scratch));
+  return bsp_spmm(A_words, M, K, B, b_dtype, ldb, N, C, ldc, plan, scratch, bsp::kNoAllocBytes, stream);
 }

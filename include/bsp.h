@@ -495,16 +495,21 @@ int bsp_csr_to_tiled(const int32_t* row_ptr, const int32_t* col_idx,
 /* bsp_spmm without a workspace argument, for callers that may not allocate
  * device memory when they run the SpMM (plugin callbacks handed only
  * pointers, hot loops that must not call the allocator, processes whose
- * device memory belongs to another allocator).  The prototype sums that bsp_spmm keeps in
- * the caller's workspace live in a static device array of 8 MiB inside the
- * library, held on every GPU that loads the library until the process exits.
+ * device memory belongs to another allocator).  It runs bsp_spmm with, as
+ * workspace, a static device array of 8 MiB inside the library, held on
+ * every GPU that loads the library until the process exits: the array holds
+ * the prototype sums and, for 16-bit B on the tensor cores, the split-K
+ * partials and the tiled copy of B whenever they fit in it (the same route
+ * bsp_spmm takes with an 8 MiB workspace, whatever the plan).
  * Limit: bsp_spmm_workspace(plan, N) must be ≤ 8 MiB (≈ n_proto * N * 4
  * bytes), else BSP_ERR_CAPACITY.  The first call on a device looks the
- * array's address up (cudaGetSymbolAddress); make that first call before any
- * stream capture.  All calls share the one array: calls that overlap on the
- * GPU (other streams, other host threads) race and must be serialised by the
- * caller.  The array keeps the last call's contents; nothing in it needs to
- * start at zero.  No counterpart in the reference.                          */
+ * array's address up (cudaGetSymbolAddress) and keeps it: make that first
+ * call before any stream capture, and do not use the library across a
+ * cudaDeviceReset (the kept address would be stale).  All calls share the
+ * one array: calls that overlap on the GPU (other streams, other host
+ * threads) race and must be serialised by the caller.  The array keeps the
+ * last call's contents; nothing in it needs to start at zero.  No
+ * counterpart in the reference.                                            */
 int bsp_spmm_noalloc(const uint32_t* A_words, int64_t M, int64_t K,
                      const void* B, int b_dtype, int64_t ldb, int64_t N,
                      float* C, int64_t ldc, const bsp_plan* plan,
