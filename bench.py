@@ -45,7 +45,8 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-secondary", action="store_true",
                    help="default run only: skip the compact c1/c3/c4/c4fb/c5 records")
-    p.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c4fb", "c5", "f1", "f2", "f3"],
+    p.add_argument("--config", default="c2",
+                   choices=["c1", "c2", "c3", "c4", "c4fb", "c5", "f1", "f2", "f3", "l2probe"],
                    help="c2 (default): clustered FP32 8192x8192x512; c1: 1024x1024x256 "
                         "integer B; c3: block-structured 16384x16384x2048 BF16 (tensor cores); "
                         "c4: 512 batched problems, N=128 BF16; c4fb: their batched forward+backward; "
@@ -133,6 +134,56 @@ def err_vs_f64(A_bits, B, C):
     rel = err[sel] / np.abs(C64[sel]) if sel.any() else np.zeros(1)
     return {"max_scaled": float(sc.max()), "mean_scaled": float(sc.mean()),
             "max_rel": float(rel.max()), "mean_rel": float(rel.mean()), "entries": int(C64.size)}
+
+
+def l2_gather_roof(dev, rows=8192, row_bytes=2048):
+    """The L2 row-gather roof (bsp_probe_gather): random row slices of a
+    16 MB buffer (the size of the clustered step's B, L2-resident) gathered
+    by 64 warps per SM, one slice in flight per warp, ~268 MB per launch.
+    Returns {slice bytes: GB/s} (best of 5 timed launches each)."""
+    import torch
+    from bitwise_spgemm_gb300 import capi
+    buf = torch.randn(rows * row_bytes // 4, device=dev)
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    n_warps = sms * 64
+    out = {}
+    for slice_bytes in (512, 1024, 2048):
+        per_warp = max(32, (268 << 20) // slice_bytes // n_warps)
+        g = torch.Generator(device=dev)
+        g.manual_seed(slice_bytes)
+        idx = torch.randint(0, rows, (n_warps * per_warp,), device=dev, generator=g, dtype=torch.int64).to(torch.int32)
+        sink = torch.zeros(n_warps, device=dev)
+        stream = torch.cuda.current_stream(dev)
+
+        def launch():
+            capi.call("bsp_probe_gather", buf.data_ptr(), rows, row_bytes, idx.data_ptr(), n_warps, per_warp,
+                      slice_bytes, sink.data_ptr(), stream.cuda_stream)
+        best = float("inf")
+        for i in range(7):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            launch()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if i >= 2:
+                best = min(best, e0.elapsed_time(e1))
+        out[slice_bytes] = n_warps * per_warp * slice_bytes / (best * 1e-3) / 1e9
+    return out
+
+
+def run_l2probe(args):
+    import torch
+    ws, rank, local = dist_setup(args)
+    dev = torch.device("cuda", local)
+    roof = l2_gather_roof(dev)
+    out = {"metric": "L2 row-gather GB/s (random slices of a 16 MB L2-resident buffer)",
+           "value": max(roof.values()), "unit": "GB/s", "n_gpus": ws, "steps": 5, "warmup": 2,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (random rows)", "config": {"workload": "l2_gather_probe_8192x2048B",
+                                                        "warps_per_sm": 64, "slices": "one in flight per warp"},
+           "by_slice_bytes": {str(k): v for k, v in roof.items()}}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
 
 
 def sample_rows(M, n):
@@ -419,6 +470,10 @@ def run_ours(args):
 
     peak, peak_kind = peaks()
     achieved = comp_bytes / (launch_ms * 1e-3) / 1e9
+    # the step's L2 gathers: prototype bits and delta entries (one B row
+    # each), one prototype-sum row read per clustered row
+    l2_bytes = (info["proto_nnz"] + info["delta_nnz"] + info["direct_nnz"] + M) * N * 4
+    roof = l2_gather_roof(dev)
     traffic = traffic_from_profiles()
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": steps,
@@ -434,7 +489,13 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_source": peak_kind,
-                     "units": "compulsory bytes of one SpMM call (proto sums + row kernel)"},
+                     "units": "compulsory bytes of one SpMM call (proto sums + row kernel)",
+                     "l2_gather": {"achieved": l2_bytes / (launch_ms * 1e-3) / 1e9,
+                                   "peak": max(roof.values()),
+                                   "frac": l2_bytes / (launch_ms * 1e-3) / 1e9 / max(roof.values()),
+                                   "unit": "GB/s", "bytes_per_step": l2_bytes,
+                                   "peak_source": "bsp_probe_gather in this run (best slice size)",
+                                   "probe_by_slice_bytes": {str(k): v for k, v in roof.items()}}},
         "e2e": {"value": e2e[False], "unit": UNIT, "h2d_bytes_per_step": bA + bB,
                 "d2h_bytes_per_step": bC, "includes": "H2D A words + B, plan build, SpMM, D2H C",
                 "pipeline": "two steps in flight: step i's D2H overlaps step i+1's uploads and plan build",
@@ -1126,6 +1187,8 @@ def main():
         run_batched(args)
     elif args.config == "c4fb":
         run_batched_fb(args)
+    elif args.config == "l2probe":
+        run_l2probe(args)
     elif args.config in ("f1", "f2", "f3"):
         run_next(args)
     elif args.config != "c2":

@@ -85,6 +85,7 @@ SIGNATURES = {
     "bsp_batched_spmm": [_P, _P],
     "bsp_batch_grad_create": [C.POINTER(ProblemGrad), _I, _I64, _I, C.POINTER(_P), _P],
     "bsp_batched_spmm_grad": [_P, _P],
+    "bsp_probe_gather": [_P, _I64, _I64, _P, _I64, _I64, _I, _P, _P],
     "bsp_spmm_t": [_P, _I64, _I64, _P, _I, _I64, _I64, _P, _I64, _P, _P, _SZ, _P],
     "bsp_sddmm": [_P, _I64, _I64, _P, _I64, _P, _I64, _I, _I64, _P, _I64, _P, _P],
     "bsp_symbolic_rows": [_P, _I64, _I64, _P, _I64, _P, _P],

@@ -515,6 +515,18 @@ int bsp_spmm_noalloc(const uint32_t* A_words, int64_t M, int64_t K,
                      float* C, int64_t ldc, const bsp_plan* plan,
                      bsp_stream_t stream);
 
+/* Measurement helper (no reference counterpart): the L2 row-gather roof of
+ * the clustered-row SpMM.  n_warps warps (a multiple of 8) each read
+ * per_warp row indices from row_idx ([n_warps][per_warp], values < rows;
+ * larger ones are skipped) and gather one slice of slice_bytes (512, 1024
+ * or 2048) bytes from the start of each row of buf ([rows][row_bytes],
+ * 16-byte aligned), one slice in flight per warp.  sink receives nothing
+ * unless the sum of the gathered values is impossible ([n_warps] floats).
+ * Time it with events: bytes = n_warps * per_warp * slice_bytes.          */
+int bsp_probe_gather(const void* buf, int64_t rows, int64_t row_bytes,
+                     const uint32_t* row_idx, int64_t n_warps, int64_t per_warp,
+                     int slice_bytes, float* sink, bsp_stream_t stream);
+
 /* Device-side status of the asynchronous kernels (0 = none; 1 = a bounded
  * mbarrier wait of the TMA-staged SpMM expired and its output is invalid).
  * Synchronises the device; clear != 0 resets the word.  No reference

@@ -68,6 +68,16 @@ def test_argument_validation_without_gpu():
     assert L.bsp_spmm_i8_workspace(3, 33, C.byref(ws)) == 0 and ws.value == 4 * 8 * 3 * 2 + 256
     assert L.bsp_spmm_i8(fake, 3, 33, 40, fake, 0, 8, 8, fake, 8, None, 0, None) == -3
     assert L.bsp_spmm_i8(fake, 3, 33, 32, fake, 0, 8, 8, fake, 8, fake, 1 << 20, None) == -1
+    # gradient batch: null out-pointer, unsupported dtype, N not a multiple of 8
+    assert L.bsp_batch_grad_create(None, 0, 8, 2, None, None) == -1
+    h = C.c_void_p()
+    assert L.bsp_batch_grad_create(None, 0, 8, 0, C.byref(h), None) == -4
+    assert L.bsp_batch_grad_create(None, 0, 12, 2, C.byref(h), None) == -2
+    assert L.bsp_batched_spmm_grad(None, None) == -1
+    # L2 gather probe: slice size, alignment, warp count
+    assert L.bsp_probe_gather(fake, 8, 2048, fake, 8, 4, 384, fake, None) == -1
+    assert L.bsp_probe_gather(P(0x10004), 8, 2048, fake, 8, 4, 512, fake, None) == -2
+    assert L.bsp_probe_gather(fake, 8, 2048, fake, 12, 4, 512, fake, None) == -1
     # plan handles
     assert L.bsp_plan_destroy(None) == 0
     assert L.bsp_plan_destroy_async(None, None) == 0
