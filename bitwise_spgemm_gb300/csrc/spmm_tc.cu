@@ -482,10 +482,11 @@ __global__ void __launch_bounds__(tc_threads(TPS), 1) k_spmm_tc(TcArgs a, const 
   // Warp w reads TMEM lanes 32*(w%4).. (a warp may only touch its own
   // quarter of the lanes) of accumulator (w/4)%2, column half w/8 of the
   // tile's 64·nbox live columns (so a narrow tile keeps all 16 warps busy);
-  // a thread holds 32 columns of one output row at a time.  Products other
-  // than the SDDMM pass them through a 32x32 tile of the (now idle) stage
-  // memory, so that each store instruction writes four whole 128-byte rows
-  // of C instead of 16 bytes in each of 32 rows.
+  // a thread holds 32 columns of one output row at a time and passes them
+  // through a 32x32 tile of the (now idle) stage memory, so that each store
+  // instruction writes four whole 128-byte rows of C instead of 16 bytes in
+  // each of 32 rows.  The SDDMM first keeps only the set bits of A's row,
+  // from the row's four words loaded once.
   if (warp < kEpiWarps) {
     const int h = (warp >> 2) & 1, q = warp & 3, cg = warp >> 3;
     const bool have = (sm.seen >> h) & 1;
@@ -510,6 +511,16 @@ __global__ void __launch_bounds__(tc_threads(TPS), 1) k_spmm_tc(TcArgs a, const 
     const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * kTcN + cg * cspan);
     float* tile = reinterpret_cast<float*>(sm.a) + warp * 32 * kEpiStride;
     const int c8_end = cspan / 8;
+    // SDDMM: the row's A words of this warp's columns (cspan = 128: four
+    // words), loaded once before the stores instead of once per 32 columns
+    uint32_t aw[4] = {0u, 0u, 0u, 0u};
+    if (kSd && live) {
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        const int64_t w = ccol / 32 + i;
+        if (i * 32 < cspan && w < gKw) aw[i] = __ldg(arow + w);
+      }
+    }
     for (int c8 = 0; c8 < c8_end; c8 += 4) {
       uint32_t r[4][8];
       if (have && ok) {
@@ -523,34 +534,25 @@ __global__ void __launch_bounds__(tc_threads(TPS), 1) k_spmm_tc(TcArgs a, const 
           for (int v = 0; v < 8; v++) r[u][v] = 0u;
       }
       if (kSd) {
-        if (!live) continue;
-        float* crow = cbase + row * cld + ccol;
+        // keep the set bits of A's row only (the row's word of these 32 columns)
+        const uint32_t wbits = aw[(c8 / 4) & 3];
 #pragma unroll
-        for (int u = 0; u < 4; u++) {
-          const int col = (c8 + u) * 8;
-          const int64_t gcol = ccol + col;
-          if (gcol >= out_cols) continue;
-          // keep the set bits of A's row only
-          const uint32_t bits = (__ldg(arow + gcol / 32) >> (gcol & 31)) & 0xffu;
+        for (int u = 0; u < 4; u++)
 #pragma unroll
           for (int v = 0; v < 8; v++)
-            if (!((bits >> v) & 1u)) r[u][v] = 0u;
-          *reinterpret_cast<float4*>(crow + col) = make_float4(
-              __uint_as_float(r[u][0]), __uint_as_float(r[u][1]), __uint_as_float(r[u][2]), __uint_as_float(r[u][3]));
-          *reinterpret_cast<float4*>(crow + col + 4) = make_float4(
-              __uint_as_float(r[u][4]), __uint_as_float(r[u][5]), __uint_as_float(r[u][6]), __uint_as_float(r[u][7]));
-        }
-        continue;
+            if (!((wbits >> (u * 8 + v)) & 1u)) r[u][v] = 0u;
       }
       if (!wlive) continue;
-      // the bit operand held 2.0 per set bit; row `lane` of the tile
+      // the bit operand held 2.0 per set bit (the SDDMM's operands are both
+      // dense: no scale); row `lane` of the tile
+      constexpr float kScale = kSd ? 1.0f : tc::kTwoScale;
 #pragma unroll
       for (int u = 0; u < 4; u++) {
         float4* t4 = reinterpret_cast<float4*>(tile + lane * kEpiStride + u * 8);
-        t4[0] = make_float4(__uint_as_float(r[u][0]) * tc::kTwoScale, __uint_as_float(r[u][1]) * tc::kTwoScale,
-                            __uint_as_float(r[u][2]) * tc::kTwoScale, __uint_as_float(r[u][3]) * tc::kTwoScale);
-        t4[1] = make_float4(__uint_as_float(r[u][4]) * tc::kTwoScale, __uint_as_float(r[u][5]) * tc::kTwoScale,
-                            __uint_as_float(r[u][6]) * tc::kTwoScale, __uint_as_float(r[u][7]) * tc::kTwoScale);
+        t4[0] = make_float4(__uint_as_float(r[u][0]) * kScale, __uint_as_float(r[u][1]) * kScale,
+                            __uint_as_float(r[u][2]) * kScale, __uint_as_float(r[u][3]) * kScale);
+        t4[1] = make_float4(__uint_as_float(r[u][4]) * kScale, __uint_as_float(r[u][5]) * kScale,
+                            __uint_as_float(r[u][6]) * kScale, __uint_as_float(r[u][7]) * kScale);
       }
       __syncwarp();
       // 8 lanes per row: rows 4*it + lane/8, 16 bytes each
