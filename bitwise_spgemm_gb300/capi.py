@@ -41,7 +41,8 @@ class PlanInfo(C.Structure):
 
 
 class Schedule(C.Structure):
-    _fields_ = [("engine", C.c_int), ("proto_path", C.c_int), ("proto_variant", C.c_int), ("ms", C.c_float)]
+    _fields_ = [("engine", C.c_int), ("proto_path", C.c_int), ("proto_variant", C.c_int), ("ms", C.c_float),
+                ("tc_stage_tiles", C.c_int), ("tc_tiled_b", C.c_int), ("tc_split", C.c_int)]
 
 
 class Problem(C.Structure):

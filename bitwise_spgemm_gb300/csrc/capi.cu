@@ -275,7 +275,9 @@ static int run_spmm(SpmmArgs a, const bsp_plan* plan, bool vec, const TuneSched&
                     size_t workspace_bytes, cudaStream_t s) {
   // Tensor cores for 16-bit B when the occupied bit tiles make a dense
   // contraction cheaper than gathering B rows.
-  if (sc.engine == 1) return launch_spmm_tc(a, plan->occ, plan->wordsT, s, workspace, workspace_bytes);
+  if (sc.engine == 1)
+    return launch_spmm_tc(a, plan->occ, plan->wordsT, s, workspace, workspace_bytes,
+                          TcForm{sc.tc_tps, sc.tc_tiled, sc.tc_split});
   const int64_t N = a.N, K = a.K;
   const bool proto = plan && plan->mode == BSP_PLAN_PROTO && vec;
   if (proto) {
@@ -396,11 +398,23 @@ int bsp_tune(const uint32_t* A_words, int64_t M, int64_t K, const void* B, int b
   const int rc = prepare_spmm(A_words, M, K, B, b_dtype, ldb, N, C, ldc, plan, s, &a, &vec, &tc_ok, &esz);
   if (rc == kDone) return BSP_ERR_INVALID_ARG;  // nothing to time
   BSP_TRY(rc);
-  // candidates: tensor cores; every prototype-kernel shape on both paths;
-  // the plain walk when the plan has no prototypes
-  TuneSched cand[1 + 7 + 8];
+  // candidates: the tensor cores in each tile form (2 or 3 K tiles per
+  // stage, B by boxes or pre-tiled, split-K by the rule or never); every
+  // prototype-kernel shape on both CUDA-core paths; the plain walk when the
+  // plan has no prototypes
+  TuneSched cand[8 + 7 + 8];
   int nc = 0;
-  if (tc_ok) cand[nc++] = TuneSched{1, 0, 0, 0.0};
+  if (tc_ok)
+    for (int tps = 2; tps <= 3; tps++)
+      for (int tiled = 0; tiled <= 1; tiled++)
+        for (int split = -1; split <= 0; split++) {
+          TuneSched t;
+          t.engine = 1;
+          t.tc_tps = tps;
+          t.tc_tiled = tiled;
+          t.tc_split = split;
+          cand[nc++] = t;
+        }
   if (plan->mode == BSP_PLAN_PROTO && vec) {
     for (int v = 0; v <= 6; v++) cand[nc++] = TuneSched{2, 0, v, 0.0};
     for (int v = 0; v <= 7; v++) cand[nc++] = TuneSched{2, 1, v, 0.0};
@@ -435,6 +449,9 @@ int bsp_tune(const uint32_t* A_words, int64_t M, int64_t K, const void* B, int b
   best->engine = cand[bi].engine;
   best->proto_path = cand[bi].proto_path;
   best->proto_variant = cand[bi].proto_variant;
+  best->tc_stage_tiles = cand[bi].tc_tps;
+  best->tc_tiled_b = cand[bi].tc_tiled;
+  best->tc_split = cand[bi].tc_split;
   best->ms = (float)cand[bi].ms;
   return BSP_OK;
 }

@@ -81,8 +81,14 @@ int launch_occupancy(const uint32_t* A, int64_t M, int64_t K, uint32_t* occ, uin
 // order (used when the rest holds tc_tiled_b_bytes(...)); else ignored.
 // At (optional): A's words column by column ([Kw][M], launch_transpose_words)
 // for coalesced word loads; null = loads from the rows.
+// form: the tile form a tuned schedule fixes (0 / -1 fields = the rule):
+// K tiles per stage (2 or 3), B pre-tiled (1) or by TMA boxes (0), split-K
+// allowed (-1) or not (0).
+struct TcForm {
+  int tps = 0, tiled = -1, split = -1;
+};
 int launch_spmm_tc(const SpmmArgs& a, const uint32_t* occ, const uint32_t* At, cudaStream_t s, void* ws = nullptr,
-                   size_t ws_bytes = 0);
+                   size_t ws_bytes = 0, TcForm form = TcForm{});
 int launch_transpose_words(const uint32_t* words, int64_t M, int64_t Kw, uint32_t* At, cudaStream_t s);
 int tc_split_count(int64_t out_rows, int64_t out_cols, int64_t red_tiles);
 size_t tc_split_bytes(int64_t out_rows, int64_t out_cols, int64_t red_tiles);

@@ -824,13 +824,13 @@ bool tiled_b_enabled() {
 }
 
 template <int MODE>
-int launch_tc(TcArgs a, cudaStream_t s, void* ws = nullptr, size_t ws_bytes = 0) {
+int launch_tc(TcArgs a, cudaStream_t s, void* ws = nullptr, size_t ws_bytes = 0, TcForm form = TcForm{}) {
   const int64_t rows = MODE == kTrans ? a.K : a.M;
   const int64_t cols = MODE == kSddmm ? a.K : a.N;
   if (rows == 0 || cols == 0) return BSP_OK;
   int splits = 1;
   size_t used = 0;
-  if (MODE != kSddmm && ws) {
+  if (MODE != kSddmm && ws && form.split != 0) {
     const int64_t red_tiles = ceil_div(MODE == kFwd ? a.K : a.M, kTcK);
     const int S = tc_split_count(rows, cols, red_tiles);
     if (S > 1 && ws_bytes >= tc_split_bytes(rows, cols, red_tiles)) {
@@ -843,8 +843,8 @@ int launch_tc(TcArgs a, cudaStream_t s, void* ws = nullptr, size_t ws_bytes = 0)
   }
   // B in tile order when the rest of the workspace holds it (else tensor boxes)
   const int64_t red_rows = MODE == kFwd ? a.K : a.M;
-  const bool tiled = MODE != kSddmm && ws && tc_tiles_b(rows) && ws_bytes >= used + tc_tiled_b_bytes(red_rows, cols) &&
-                     tiled_b_enabled();
+  const bool room = MODE != kSddmm && ws && ws_bytes >= used + tc_tiled_b_bytes(red_rows, cols);
+  const bool tiled = room && (form.tiled >= 0 ? form.tiled == 1 : tc_tiles_b(rows) && tiled_b_enabled());
   const dim3 grid((unsigned)ceil_div(rows, kCtaM), (unsigned)ceil_div(cols, kTcN), (unsigned)splits);
   if (ceil_div(cols, kTcN) > 65535 || ceil_div(rows, kCtaM) > 0x7fffffff) return BSP_ERR_CAPACITY;
   if (a.N > INT32_MAX || a.M > INT32_MAX || a.K > INT32_MAX) return BSP_ERR_CAPACITY;
@@ -875,7 +875,7 @@ int launch_tc(TcArgs a, cudaStream_t s, void* ws = nullptr, size_t ws_bytes = 0)
   if (a.bdt != BSP_BF16 && a.bdt != BSP_F16) return BSP_ERR_UNSUPPORTED;
   bool launched = false;
   if constexpr (MODE != kSddmm) {  // (the SDDMM has one stage form)
-    if (three_tiles(rows)) {
+    if (form.tps ? form.tps == 3 : three_tiles(rows)) {
       if (a.bdt == BSP_BF16) BSP_TRY((launch_mode<__nv_bfloat16, MODE, 3>(a, ma, mb, grid, s)));
       else BSP_TRY((launch_mode<__half, MODE, 3>(a, ma, mb, grid, s)));
       launched = true;
@@ -897,7 +897,7 @@ int launch_tc(TcArgs a, cudaStream_t s, void* ws = nullptr, size_t ws_bytes = 0)
 }  // namespace
 
 int launch_spmm_tc(const SpmmArgs& sa, const uint32_t* occ, const uint32_t* At, cudaStream_t s, void* ws,
-                   size_t ws_bytes) {
+                   size_t ws_bytes, TcForm form) {
   TcArgs a = {};
   a.At = At;
   a.A = sa.A;
@@ -912,7 +912,7 @@ int launch_spmm_tc(const SpmmArgs& sa, const uint32_t* occ, const uint32_t* At, 
   a.occ = occ;
   a.occ_words = tc_occupancy_words(sa.K);
   a.bdt = sa.bdt;
-  return launch_tc<kFwd>(a, s, ws, ws_bytes);
+  return launch_tc<kFwd>(a, s, ws, ws_bytes, form);
 }
 
 int launch_spmm_t_tc(const uint32_t* A, int64_t M, int64_t K, const void* G, int gdt, int64_t ldg, int64_t N,

@@ -1,8 +1,10 @@
 // tune.cu — the autotuner's cache: measured SpMM schedules per shape bucket.
 //
-// A schedule says which engine runs the SpMM (tensor cores or CUDA cores)
-// and, on the CUDA cores, which prototype-row kernel (register gathers or
-// TMA-staged slices) and which of its shapes.  bsp_tune (capi.cu) times the
+// A schedule says which engine runs the SpMM (tensor cores or CUDA cores —
+// the tensor-core density threshold of the bucket), on the tensor cores
+// which tile form (K tiles per stage, B by TMA boxes or pre-tiled, split-K
+// or not), and on the CUDA cores which prototype-row kernel (register
+// gathers or TMA-staged slices) and which of its shapes.  bsp_tune (capi.cu) times the
 // candidates on the caller's data and stores the fastest here under a bucket
 // key (log2 sizes, density in half octaves, dtype, plan mode); bsp_spmm then
 // looks the bucket up before its cost model.  The cache lives in the process
@@ -12,10 +14,12 @@
 // file.  A file that does not parse is ignored as a whole.
 //
 // File format (JSON, one entry per line):
-//   {"bsp_tune_cache": 1, "entries": [
-//    {"key": "M13K13N9d9t0p2", "engine": 2, "proto_path": 0, "proto_variant": 4, "ms": 0.0328},
+//   {"bsp_tune_cache": 2, "entries": [
+//    {"key": "M13K13N9d9t0p2", "engine": 2, "proto_path": 0, "proto_variant": 4, "tc_tps": 0,
+//     "tc_tiled": -1, "tc_split": -1, "ms": 0.0328},
 //    ...
 //   ]}
+// (one entry per line; a version-1 file, without the tile form, does not parse)
 #include <unistd.h>
 
 #include <atomic>
@@ -52,7 +56,7 @@ bool parse_file(const char* path, std::map<std::string, TuneSched>& out) {
   char line[512];
   bool header = false, closed = false, ok = true;
   while (fgets(line, sizeof line, f)) {
-    if (strstr(line, "\"bsp_tune_cache\": 1")) {
+    if (strstr(line, "\"bsp_tune_cache\": 2")) {
       header = true;
       continue;
     }
@@ -60,10 +64,13 @@ bool parse_file(const char* path, std::map<std::string, TuneSched>& out) {
       char key[96];
       TuneSched t;
       double ms = 0;
-      if (sscanf(line, " {\"key\": \"%95[^\"]\", \"engine\": %d, \"proto_path\": %d, \"proto_variant\": %d, \"ms\": %lf",
-                 key, &t.engine, &t.proto_path, &t.proto_variant, &ms) != 5 ||
+      if (sscanf(line,
+                 " {\"key\": \"%95[^\"]\", \"engine\": %d, \"proto_path\": %d, \"proto_variant\": %d, "
+                 "\"tc_tps\": %d, \"tc_tiled\": %d, \"tc_split\": %d, \"ms\": %lf",
+                 key, &t.engine, &t.proto_path, &t.proto_variant, &t.tc_tps, &t.tc_tiled, &t.tc_split, &ms) != 8 ||
           (t.engine != 1 && t.engine != 2) || t.proto_path < 0 || t.proto_path > 1 || t.proto_variant < 0 ||
-          t.proto_variant > 7) {
+          t.proto_variant > 7 || (t.tc_tps != 0 && t.tc_tps != 2 && t.tc_tps != 3) || t.tc_tiled < -1 ||
+          t.tc_tiled > 1 || t.tc_split < -1 || t.tc_split > 0) {
         ok = false;
         break;
       }
@@ -90,12 +97,15 @@ bool write_file(const char* path, const std::map<std::string, TuneSched>& m) {
   std::string tmp = std::string(path) + ".tmp" + std::to_string((long)getpid());
   FILE* f = fopen(tmp.c_str(), "w");
   if (!f) return false;
-  bool ok = fprintf(f, "{\"bsp_tune_cache\": 1, \"entries\": [\n") > 0;
+  bool ok = fprintf(f, "{\"bsp_tune_cache\": 2, \"entries\": [\n") > 0;
   size_t i = 0;
   for (const auto& kv : m) {
-    ok = ok && fprintf(f, " {\"key\": \"%s\", \"engine\": %d, \"proto_path\": %d, \"proto_variant\": %d, \"ms\": %.6f}%s\n",
+    ok = ok && fprintf(f,
+                       " {\"key\": \"%s\", \"engine\": %d, \"proto_path\": %d, \"proto_variant\": %d, "
+                       "\"tc_tps\": %d, \"tc_tiled\": %d, \"tc_split\": %d, \"ms\": %.6f}%s\n",
                        kv.first.c_str(), kv.second.engine, kv.second.proto_path, kv.second.proto_variant,
-                       kv.second.ms, ++i < m.size() ? "," : "") > 0;
+                       kv.second.tc_tps, kv.second.tc_tiled, kv.second.tc_split, kv.second.ms,
+                       ++i < m.size() ? "," : "") > 0;
   }
   ok = ok && fprintf(f, "]}\n") > 0;
   ok = (fclose(f) == 0) && ok;

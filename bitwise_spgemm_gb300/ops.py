@@ -223,8 +223,9 @@ def sddmm(words, M, K, G, X, plan=None, out=None):
 def tune(words, K, B, plan, out=None, workspace=None):
     """Time every SpMM schedule for this plan and operands (bsp_tune), keep
     the fastest in the library's per-shape-bucket cache and return it as a
-    dict (engine 1 = tensor cores, 2 = CUDA cores; prototype path and shape;
-    ms).  ``out`` ends holding the product."""
+    dict (engine 1 = tensor cores, 2 = CUDA cores; the tensor-core tile form:
+    K tiles per stage, B pre-tiled or by boxes, split-K; the prototype path
+    and shape; ms).  ``out`` ends holding the product."""
     M = words.shape[0]
     ldb = _rowmajor(B, "B")
     N = B.shape[1]
@@ -237,6 +238,7 @@ def tune(words, K, B, plan, out=None, workspace=None):
     call("bsp_tune", _p(words), M, K, _p(B), _DT[B.dtype], ldb, N, _p(out), out.stride(0), plan.handle,
          _p(workspace), workspace.numel() * workspace.element_size(), _stream(), C.byref(best))
     return {"engine": best.engine, "proto_path": best.proto_path, "proto_variant": best.proto_variant,
+            "tc_stage_tiles": best.tc_stage_tiles, "tc_tiled_b": best.tc_tiled_b, "tc_split": best.tc_split,
             "ms": best.ms}
 
 

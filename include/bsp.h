@@ -311,20 +311,27 @@ int bsp_batched_spmm_grad(const bsp_batch* batch, bsp_stream_t stream);
 /* Autotuner                                                                */
 /* ======================================================================== */
 
-/* A measured SpMM schedule: engine 1 = tensor cores, 2 = CUDA cores; on the
- * CUDA cores with a prototype plan, proto_path 0 = register gathers / 1 =
- * TMA-staged slices and proto_variant = that kernel's shape; ms = its time. */
+/* A measured SpMM schedule: engine 1 = tensor cores, 2 = CUDA cores (per
+ * shape bucket, this is the tensor-core density threshold); on the tensor
+ * cores the tile form (K tiles per stage, B pre-tiled or by TMA boxes,
+ * split-K or not); on the CUDA cores with a prototype plan, proto_path 0 =
+ * register gathers / 1 = TMA-staged slices and proto_variant = that
+ * kernel's shape (columns per warp, gathers in flight, CTAs per SM); ms =
+ * its time.                                                                 */
 typedef struct bsp_schedule {
   int engine;
   int proto_path;
   int proto_variant;
   float ms;
+  int tc_stage_tiles;  /* tensor cores: K tiles per stage (2 or 3; 0 = rule) */
+  int tc_tiled_b;      /* tensor cores: B copied into tile order (1), TMA boxes (0), rule (-1) */
+  int tc_split;        /* tensor cores: split-K by the rule (-1) or never (0) */
 } bsp_schedule;
 
 /* Times every candidate schedule of bsp_spmm for this plan and these
- * operands (tensor cores when allowed; each prototype-kernel shape on both
- * paths; 2 warm-up + 5 timed runs each, CUDA events on `stream`, which it
- * synchronises), leaves C holding the fastest one's result, returns it in
+ * operands (the tensor cores in 8 tile forms when allowed; each
+ * prototype-kernel shape on both paths; 2 warm-up + 5 timed runs each, CUDA
+ * events on `stream`, which it synchronises), leaves C holding the fastest one's result, returns it in
  * *best and caches it for the shape bucket (log2 of M, K, N; density in half
  * octaves; dtype; plan mode).  bsp_spmm uses a cached schedule for its
  * bucket unless BSP_TC, BSP_PROTO_PATH or BSP_PROTO_VARIANT force a choice.

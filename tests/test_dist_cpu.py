@@ -29,9 +29,9 @@ def _rank(rank, port, q):
     import bench
     import torch.distributed as dist
     # a tiny stand-in for the CPU sample (the real one runs for seconds)
-    bench.workload = lambda: ({"name": "stand-in"}, 1_000_000, (0, 0, 0))
+    bench.workload = lambda: ({"name": "stand-in", "M": 8}, 1_000_000, (0, 0, 0))
     bench.cpu_sample_rows = lambda cfg, seconds, threads: 8
-    bench.cpu_reference = lambda cfg, rows, threads: (0.001, "stand-in sample")
+    bench.cpu_reference = lambda cfg, rows, threads: (0.001, 0.001, "stand-in sample")
     out = io.StringIO()
     with contextlib.redirect_stdout(out):
         bench.run_reference(bench.parse())

@@ -198,3 +198,41 @@ def test_batched_grad_validation():
         ops.BatchGrad([(w, 60, X, G, None, dA)])
     fwd = ops.Batch([(w, 60, X, torch.zeros((64, 128), device="cuda"))])
     assert capi.lib().bsp_batched_spmm_grad(fwd._h, None) == -1  # BSP_ERR_INVALID_ARG
+
+
+@pytest.mark.slow
+def test_batched_set_real_shapes_against_fp64():
+    """Every 32nd problem of the 512-problem batched set itself (M, K
+    log-uniform in [64, 4096], density U(0.01, 0.3), N = 128, seeds 7+i):
+    forward through the persistent kernel, and the backward pass with the
+    set's seeded gradients, against FP64 (BF16 products are exact, FP32
+    accumulation: scaled error ≤ 1e-4)."""
+    idx = list(range(0, 512, 32))
+    probs = [W.config4_problem(i) for i in idx]
+    fwd, grad = [], []
+    for i, pr in zip(idx, probs):
+        M, K = pr["M"], pr["K"]
+        wd = torch.from_numpy(np.ascontiguousarray(pr["words"]).view(np.int32)).cuda()
+        X = bf16_dev(pr["B"])
+        G = bf16_dev(W.config4_grad(pr, i))
+        fwd.append((wd, K, X, torch.full((M, 128), float("nan"), device="cuda")))
+        grad.append((wd, K, X, G, torch.full((K, 128), float("nan"), device="cuda"),
+                     torch.full((M, K), float("nan"), device="cuda")))
+    bf, bg = ops.Batch(fwd), ops.BatchGrad(grad)
+    bf.run()
+    bg.run()
+    torch.cuda.synchronize()
+    assert capi.device_status() == 0
+    for i, pr, f, g in zip(idx, probs, fwd, grad):
+        M, K, words = pr["M"], pr["K"], pr["words"]
+        X, G = W.bf16_bits_to_f32(pr["B"]), W.bf16_bits_to_f32(W.config4_grad(pr, i))
+        mx, _, _ = O.rel_errors(f[3].cpu().numpy(), O.spmm_f64(words, K, X), O.spmm_abs_f64(words, K, X))
+        assert mx <= TOL, (i, "Y", mx)
+        mx, _, _ = O.rel_errors(g[4].cpu().numpy(), O.spmm_t_f64(words, M, K, G), O.spmm_t_f64(words, M, K, np.abs(G)))
+        assert mx <= TOL, (i, "dX", mx)
+        A = W.unpack_bits(words, K)
+        dA = g[5].cpu().numpy()
+        v64 = O.sddmm_f64(words, M, K, G, X)
+        sc = (np.abs(G.astype(np.float64)) @ np.abs(X.astype(np.float64)).T)[A]
+        assert np.all(dA[~A] == 0.0)
+        assert (np.abs(dA[A] - v64) / np.where(sc > 0, sc, 1.0)).max() <= TOL, (i, "dA")

@@ -90,6 +90,47 @@ def test_cache_file_written_through_env(tmp_path):
     env = dict(os.environ, BSP_TUNE_CACHE=str(path))
     r = subprocess.run([sys.executable, "-c", code, "tune"], env=env, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
-    assert path.exists() and '"bsp_tune_cache": 1' in path.read_text()
+    assert path.exists() and '"bsp_tune_cache": 2' in path.read_text()
     r2 = subprocess.run([sys.executable, "-c", code, "read"], env=env, capture_output=True, text=True, timeout=300)
     assert r2.returncode == 0 and "entries 1" in r2.stdout, r2.stdout + r2.stderr
+
+
+@pytest.mark.parametrize("M", [512, 8192])
+def test_tensor_core_tile_forms_from_the_cache(M, tmp_path):
+    """Each tensor-core tile form a cache entry can name (2 or 3 K tiles per
+    stage, B by boxes or pre-tiled, split-K by the rule or never) gives the
+    product within the tensor-core tolerance of FP64; tuning picks one of
+    them and records it.  512 rows: the split-K rule applies; 8192 rows:
+    B is pre-tiled by the rule."""
+    import ctypes
+    import re
+    rng = np.random.default_rng(M)
+    K, N = 2048, 256
+    bits, _ = W.block_bits(M, K, p_tile=0.3)
+    words = W.pack_bits(bits)
+    wd = words_dev(words)
+    plan = ops.Plan(wd, K)
+    Bf = rng.standard_normal((K, N), dtype=np.float32)
+    Bb = W.f32_to_bf16_bits(Bf)
+    B, Bx = bf16_dev(Bb), W.bf16_bits_to_f32(Bb)
+    C64, Cabs = O.spmm_f64(words, K, Bx), O.spmm_abs_f64(words, K, Bx)
+    best = ops.tune(wd, K, B, plan)
+    if best["engine"] == 1:
+        assert best["tc_stage_tiles"] in (2, 3) and best["tc_tiled_b"] in (0, 1) and best["tc_split"] in (-1, 0)
+    path = tmp_path / "cache.json"
+    assert capi.lib().bsp_tune_cache_save(str(path).encode()) == 0
+    text = path.read_text()
+    n = ctypes.c_int(0)
+    for tps in (2, 3):
+        for tiled in (0, 1):
+            for split in (-1, 0):
+                t = re.sub(r'"engine": \d', '"engine": 1', text)
+                t = re.sub(r'"tc_tps": -?\d', '"tc_tps": %d' % tps, t)
+                t = re.sub(r'"tc_tiled": -?\d', '"tc_tiled": %d' % tiled, t)
+                t = re.sub(r'"tc_split": -?\d', '"tc_split": %d' % split, t)
+                path.write_text(t)
+                assert capi.lib().bsp_tune_cache_load(str(path).encode(), ctypes.byref(n)) == 0
+                C = ops.spmm(wd, K, B, plan=plan).cpu().numpy()
+                mx, _, _ = O.rel_errors(C, C64, Cabs)
+                assert mx <= 1e-4, (tps, tiled, split, mx)
+    assert capi.device_status() == 0

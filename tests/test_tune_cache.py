@@ -6,9 +6,14 @@ import os
 
 from bitwise_spgemm_gb300 import capi
 
-GOOD = """{"bsp_tune_cache": 1, "entries": [
- {"key": "M13K13N9d9t0p2", "engine": 2, "proto_path": 0, "proto_variant": 4, "ms": 0.032800},
- {"key": "M14K14N11d4t2p1", "engine": 1, "proto_path": 0, "proto_variant": 0, "ms": 0.787000}
+GOOD = """{"bsp_tune_cache": 2, "entries": [
+ {"key": "M13K13N9d9t0p2", "engine": 2, "proto_path": 0, "proto_variant": 4, "tc_tps": 0, "tc_tiled": -1, "tc_split": -1, "ms": 0.032800},
+ {"key": "M14K14N11d4t2p1", "engine": 1, "proto_path": 0, "proto_variant": 0, "tc_tps": 3, "tc_tiled": 1, "tc_split": 0, "ms": 0.595000}
+]}
+"""
+# a file in the first format (no tile form) is refused as a whole
+OLD = """{"bsp_tune_cache": 1, "entries": [
+ {"key": "M13K13N9d9t0p2", "engine": 2, "proto_path": 0, "proto_variant": 4, "ms": 0.032800}
 ]}
 """
 
@@ -29,7 +34,9 @@ def test_cache_load_save_and_corrupt_files(tmp_path):
     # malformed files: truncated, a bad engine, junk between entries
     for bad in (GOOD[: len(GOOD) // 2],
                 GOOD.replace('"engine": 1', '"engine": 7'),
-                GOOD.replace("]}", "garbage\n]}")):
+                GOOD.replace('"tc_tps": 3', '"tc_tps": 5'),
+                GOOD.replace("]}", "garbage\n]}"),
+                OLD):
         p = tmp_path / "bad.json"
         p.write_text(bad)
         assert L.bsp_tune_cache_load(str(p).encode(), C.byref(n)) == -1
