@@ -40,7 +40,7 @@ def parse():
     p.add_argument("--steps", type=int, default=200)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--e2e-steps", type=int, default=10)
+    p.add_argument("--e2e-steps", type=int, default=50)
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-secondary", action="store_true",
@@ -184,6 +184,37 @@ def run_l2probe(args):
            "by_slice_bytes": {str(k): v for k, v in roof.items()}}
     if rank == 0:
         print(json.dumps(out), flush=True)
+
+
+def e2e_native(cfg, words_np, B_np, C_ref, args, local, ws, comp_bytes):
+    """Runs the C++ end-to-end loop (bsp_e2e) on this rank's GPU, with the
+    plan built every step and with the plan reused.  Returns ({reuse: GB/s},
+    whether its last C equals C_ref bit for bit, the driver's lines)."""
+    import tempfile
+    from bitwise_spgemm_gb300 import build as libbuild
+    exe = libbuild.E2E if os.path.exists(libbuild.E2E) else libbuild.build_e2e()
+    env = dict(os.environ)
+    vis = env.get("CUDA_VISIBLE_DEVICES")
+    ids = [x for x in vis.split(",") if x.strip()] if vis else None
+    env["CUDA_VISIBLE_DEVICES"] = ids[local] if ids and local < len(ids) else str(local)
+    out, runs, match = {}, {}, True
+    with tempfile.TemporaryDirectory() as d:
+        np.ascontiguousarray(words_np).tofile(os.path.join(d, "words.bin"))
+        np.ascontiguousarray(B_np, np.float32).tofile(os.path.join(d, "B.bin"))
+        M, K, N = cfg["M"], cfg["K"], cfg["N"]
+        for mode, key in ((0, False), (1, True), (2, "copies")):
+            r = subprocess.run([exe, d, str(M), str(K), str(N), str(args.e2e_steps), "3", str(mode)],
+                               capture_output=True, text=True, timeout=600, env=env)
+            if r.returncode != 0:
+                raise RuntimeError("bsp_e2e failed: " + r.stderr[-400:])
+            line = json.loads(r.stdout.strip().splitlines()[-1])
+            runs[("built", "reused", "copies_only")[mode]] = line
+            ms = max_over_ranks(ws, line["ms_per_step"])
+            out[key] = ws * comp_bytes / (ms * 1e-3) / 1e9
+            if mode < 2:
+                Ch = np.fromfile(os.path.join(d, "C.bin"), np.float32).reshape(M, N)
+                match = match and bool(np.array_equal(Ch, C_ref)) and line["device_status"] == 0
+    return out, match, runs
 
 
 def sample_rows(M, n):
@@ -415,58 +446,10 @@ def run_ours(args):
     err64 = err_vs_f64(W.unpack_bits(cfg["words"][rows], K), B_np, Cs[0].cpu().numpy()[rows])
     err64["sample"] = "%d rows evenly spaced over %d" % (len(rows), M)
 
-    # e2e through the public API: pinned host A words and B in, C out, plan
-    # built per step.  Steps are pipelined two deep, as a serving loop runs
-    # them: step i's C download runs on a copy stream while step i+1 uploads
-    # its inputs and builds its plan (each step still moves all its bytes).
-    h_words = torch.from_numpy(words_np).pin_memory()
-    h_B = torch.from_numpy(B_np).pin_memory()
-    h_C = [torch.empty((M, N), dtype=torch.float32).pin_memory() for _ in range(2)]
-    d_words = [torch.empty_like(words) for _ in range(2)]
-    d_B = [torch.empty((K, N), device=dev) for _ in range(2)]
-    d_C = [torch.empty((M, N), device=dev) for _ in range(2)]
-    side = torch.cuda.Stream(device=dev)
-    d2h = torch.cuda.Stream(device=dev)
-    downloaded = [torch.cuda.Event() for _ in range(2)]  # set j's C is on the host
-    used = [torch.cuda.Event() for _ in range(2)]        # set j's SpMM has run
-
-    def e2e_step(i, reuse_plan):
-        # A's words first (the plan needs them); B goes up at the same time on
-        # a side stream, once the SpMM that last read this buffer has run, and
-        # the SpMM waits for that copy
-        j = i % 2
-        cur = torch.cuda.current_stream()
-        cur.wait_event(downloaded[j])  # this buffer set's previous C is on the host
-        d_words[j].copy_(h_words, non_blocking=True)
-        side.wait_event(used[j])
-        with torch.cuda.stream(side):
-            d_B[j].copy_(h_B, non_blocking=True)
-        p = plan if reuse_plan else ops.Plan(d_words[j], K)
-        cur.wait_stream(side)
-        ops.spmm(d_words[j], K, d_B[j], plan=p, out=d_C[j], workspace=wsp if reuse_plan else None)
-        used[j].record(cur)
-        if not reuse_plan:
-            p.close_async()
-        d2h.wait_stream(cur)
-        with torch.cuda.stream(d2h):
-            h_C[j].copy_(d_C[j], non_blocking=True)
-            downloaded[j].record(d2h)
-
-    e2e = {}
-    last = 0
-    for reuse in (False, True):
-        for i in range(2):
-            e2e_step(i, reuse)
-        torch.cuda.synchronize()
-        barrier(ws)
-        t0 = time.perf_counter()
-        for i in range(args.e2e_steps):
-            e2e_step(i, reuse)
-            last = i % 2
-        torch.cuda.synchronize()
-        dt = max_over_ranks(ws, (time.perf_counter() - t0) / args.e2e_steps)
-        e2e[reuse] = ws * comp_bytes / dt / 1e9
-    e2e_matches = bool(np.array_equal(h_C[last].numpy(), Cs[0].cpu().numpy()))
+    # e2e through the C ABI from a C++ serving loop (harness/bsp_e2e): pinned
+    # host A words and B in, plan, SpMM, C out, per step, two steps in
+    # flight; once with the plan built every step, once reused
+    e2e, e2e_matches, e2e_runs = e2e_native(cfg, words_np, B_np, Cs[0].cpu().numpy(), args, local, ws, comp_bytes)
 
     peak, peak_kind = peaks()
     achieved = comp_bytes / (launch_ms * 1e-3) / 1e9
@@ -499,7 +482,14 @@ def run_ours(args):
         "e2e": {"value": e2e[False], "unit": UNIT, "h2d_bytes_per_step": bA + bB,
                 "d2h_bytes_per_step": bC, "includes": "H2D A words + B, plan build, SpMM, D2H C",
                 "pipeline": "two steps in flight: step i's D2H overlaps step i+1's uploads and plan build",
-                "plan_reused_value": e2e[True]},
+                "caller": "C++ serving loop through the C ABI (bitwise_spgemm_gb300/harness/bsp_e2e.cpp), "
+                          "wall clock over %d steps" % args.e2e_steps,
+                "plan_reused_value": e2e[True],
+                "link_roof": {"value": e2e["copies"], "unit": UNIT,
+                              "what": "the same loop's uploads and downloads alone (no plan, no SpMM)",
+                              "frac_plan_built": e2e[False] / e2e["copies"],
+                              "frac_plan_reused": e2e[True] / e2e["copies"]},
+                "runs": e2e_runs},
         "gpu_launches": steps * kernels_per_step,
         "clocks": clocks,
         "max_rel_diff_vs_direct": err,

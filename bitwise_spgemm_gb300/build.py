@@ -65,6 +65,22 @@ def build_harness(force=False):
     return HARNESS
 
 
+E2E_SRC = os.path.join(PKG, "harness", "bsp_e2e.cpp")
+E2E = os.path.join(PKG, "harness", "bsp_e2e")
+
+
+def build_e2e(force=False):
+    """The C++ end-to-end serving loop (C ABI only), linked like the harness."""
+    newest = max(os.path.getmtime(p) for p in [E2E_SRC, LIB] + glob.glob(os.path.join(INCLUDE, "*.h")))
+    if not force and os.path.exists(E2E) and os.path.getmtime(E2E) >= newest:
+        return E2E
+    tmp = E2E + ".tmp%d" % os.getpid()
+    subprocess.check_call([nvcc(), "-O2", "-std=c++17", "-I", INCLUDE, E2E_SRC, "-o", tmp, "-L", PKG, "-lbsp",
+                           "-Xlinker", "-rpath,$ORIGIN/.."])
+    os.replace(tmp, E2E)
+    return E2E
+
+
 CUSPARSE_SRC = os.path.join(PKG, "baselines", "cusparse_spmm.cpp")
 CUSPARSE_LIB = os.path.join(PKG, "libbsp_cusparse.so")
 
@@ -101,6 +117,7 @@ def build(force=False, jobs=None):
         subprocess.check_call([nvcc()] + ARCH + ["-shared", "-o", tmp] + objs)
         os.replace(tmp, LIB)
     build_harness(force)
+    build_e2e(force)
     build_cusparse_baseline(force)
     return LIB
 
