@@ -338,3 +338,25 @@ def test_plan_with_many_rows():
     s0 = ops.symbolic_rows(wd, K, bd, 96)
     assert torch.equal(s1, s0)
     assert capi.device_status() == 0
+
+
+def test_probe_gather_runs_and_checks_its_arguments():
+    """The L2 gather roof probe (bsp_probe_gather): a small launch with every
+    slice size returns OK and leaves the sink untouched (the gathered sum is
+    never the impossible value); indices past the buffer are skipped."""
+    import ctypes
+    rows, row_bytes = 256, 2048
+    buf = torch.randn(rows * row_bytes // 4, device="cuda")
+    n_warps, per_warp = 64, 40
+    idx = torch.randint(0, rows + 8, (n_warps * per_warp,), device="cuda", dtype=torch.int32)
+    sink = torch.zeros(n_warps, device="cuda")
+    for sb in (512, 1024, 2048):
+        st = capi.lib().bsp_probe_gather(ctypes.c_void_p(buf.data_ptr()), rows, row_bytes,
+                                         ctypes.c_void_p(idx.data_ptr()), n_warps, per_warp, sb,
+                                         ctypes.c_void_p(sink.data_ptr()), None)
+        assert st == 0
+    torch.cuda.synchronize()
+    assert float(sink.abs().max()) == 0.0
+    assert capi.lib().bsp_probe_gather(ctypes.c_void_p(buf.data_ptr()), rows, 1024,
+                                       ctypes.c_void_p(idx.data_ptr()), n_warps, per_warp, 2048,
+                                       ctypes.c_void_p(sink.data_ptr()), None) == -2
