@@ -337,7 +337,7 @@ __global__ void __launch_bounds__(kConsThreads) k_consensus(const uint32_t* __re
                                                             const int32_t* __restrict__ csize,
                                                             int H, uint32_t seed, uint32_t* __restrict__ cons,
                                                             uint32_t* akeys, int32_t* avals, uint32_t tmask,
-                                                            unsigned long long* stats) {
+                                                            unsigned long long* stats, int32_t* cons_cnt) {
   static_assert(kConsRowChunk / kConsGroups < (1 << kConsPlanes), "planes");
   __shared__ uint32_t wmin[kMaxHashes][kConsThreads / 32];
   __shared__ unsigned wpop[kConsThreads / 32];
@@ -422,6 +422,7 @@ __global__ void __launch_bounds__(kConsThreads) k_consensus(const uint32_t* __re
   if (threadIdx.x == 0) {
     unsigned long long total = 0;
     for (int i = 0; i < kConsThreads / 32; i++) total += wpop[i];
+    cons_cnt[c] = (int32_t)total;
     if (total) {
       atomicAdd(stats + 4, total);
       atomicMax(stats + 7, total);
@@ -513,6 +514,35 @@ __global__ void __launch_bounds__(256) k_finalize_rows(
   }
 }
 
+
+// Warp per prototype: its set columns in ascending order into
+// cons_idx[cons_ptr[c] ..] (the list the prototype-sum kernel walks).
+__global__ void __launch_bounds__(256) k_cons_fill(const uint32_t* __restrict__ cons, int64_t n_proto, int Kw,
+                                                   const int32_t* __restrict__ cons_ptr, uint32_t* __restrict__ idx) {
+  const int lane = threadIdx.x & 31;
+  const int64_t c = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  if (c >= n_proto) return;
+  const uint32_t* p = cons + c * Kw;
+  int base = cons_ptr[c];
+  for (int w0 = 0; w0 < Kw; w0 += 32) {
+    const int w = w0 + lane;
+    uint32_t x = w < Kw ? p[w] : 0u;
+    const int cnt = __popc(x);
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(kFull, incl, o);
+      if (lane >= o) incl += y;
+    }
+    int pos = base + incl - cnt;
+    while (x) {
+      const int b = __ffs(x) - 1;
+      x &= x - 1;
+      idx[pos++] = (uint32_t)(w * 32 + b);
+    }
+    base += __shfl_sync(kFull, incl, 31);
+  }
+}
 
 // Warp per clustered row: delta entries in ascending column order.
 __global__ void __launch_bounds__(256) k_delta_fill(const uint32_t* __restrict__ words, int64_t M,
@@ -873,6 +903,7 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
   const size_t p_cl = ptake(sizeof(int32_t) * M);
   const size_t p_dp = ptake(sizeof(int32_t) * (M + 1));
   const size_t p_cons = ptake(sizeof(uint32_t) * ncl * Kw);
+  const size_t p_cptr = ptake(sizeof(int32_t) * (ncl + 1));
   const size_t p_dl = ptake(sizeof(int32_t) * M);
   void* parena = nullptr;
   BSP_CUDA(plan_alloc(&parena, poff ? poff : 16, s, &plan->arena_pooled));
@@ -881,6 +912,7 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
   plan->row_cluster = (int32_t*)(Pa + p_cl);
   plan->delta_ptr = (int32_t*)(Pa + p_dp);
   plan->cons = (uint32_t*)(Pa + p_cons);
+  plan->cons_ptr = (int32_t*)(Pa + p_cptr);
   plan->direct_list = (int32_t*)(Pa + p_dl);
   plan->n_proto = ncl;
 
@@ -891,6 +923,7 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
     const size_t q_csize = take2(sizeof(int32_t) * ncl);
     const size_t q_cstart = take2(sizeof(int32_t) * ncl);
     const size_t q_cursor = take2(sizeof(int32_t) * ncl);
+    const size_t q_ccnt = take2(sizeof(int32_t) * ncl);
     const size_t q_rows = take2(sizeof(int32_t) * M);
     const size_t q_akeys = take2(sizeof(uint32_t) * asize * H);
     const size_t q_avals = take2(sizeof(int32_t) * asize * H);
@@ -900,6 +933,7 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
     int32_t* csize = (int32_t*)(T2 + q_csize);
     int32_t* cstart = (int32_t*)(T2 + q_cstart);
     int32_t* cursor = (int32_t*)(T2 + q_cursor);
+    int32_t* ccnt = (int32_t*)(T2 + q_ccnt);
     int32_t* crows = (int32_t*)(T2 + q_rows);
     uint32_t* akeys = (uint32_t*)(T2 + q_akeys);
     int32_t* avals = (int32_t*)(T2 + q_avals);
@@ -908,7 +942,9 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
     k_cluster_rows<<<tgrid, 256, 0, s>>>(slot, cnt, lead, cid, coff, M, min_rows, plan->row_cluster, csize, cstart,
                                          cursor, crows);
     k_consensus<<<(unsigned)ncl, kConsThreads, 0, s>>>(words, Kw, crows, cstart, csize, H, prm->seed, plan->cons,
-                                                      akeys, avals, asize - 1, stats);
+                                                      akeys, avals, asize - 1, stats, ccnt);
+    BSP_LAUNCHED();
+    BSP_TRY(launch_scan_i32(ccnt, ncl, plan->cons_ptr, scanws, s));
     k_finalize_rows<<<wgrid, 256, 0, s>>>(words, M, Kw, H, sig, nnz, plan->cons, ncl, akeys, avals,
                                           asize - 1, plan->row_cluster, dcnt, stats);
     BSP_LAUNCHED();
@@ -949,11 +985,19 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
     k_direct_scatter<<<tgrid, 256, 0, s>>>(flag, cid, M, plan->direct_list);
     BSP_LAUNCHED();
   }
-  if (mode == BSP_PLAN_PROTO && plan->delta_nnz > 0) {
-    BSP_CUDA(plan_alloc(&plan->delta_arena, sizeof(uint32_t) * plan->delta_nnz, s, &plan->delta_pooled));
+  // the prototypes' column lists (int32 offsets: kept only below 2^31 entries)
+  const int64_t n_list = plan->proto_nnz < INT_MAX ? plan->proto_nnz : 0;
+  if (mode == BSP_PLAN_PROTO && plan->delta_nnz + n_list > 0) {
+    // one block: the delta lists, then the prototypes' column lists
+    BSP_CUDA(plan_alloc(&plan->delta_arena, sizeof(uint32_t) * (plan->delta_nnz + n_list), s,
+                        &plan->delta_pooled));
     plan->delta_idx = (uint32_t*)plan->delta_arena;
-    k_delta_fill<<<wgrid, 256, 0, s>>>(words, M, Kw, plan->cons, plan->row_cluster,
-                                       plan->delta_ptr, plan->delta_idx);
+    plan->cons_idx = n_list > 0 ? plan->delta_idx + plan->delta_nnz : nullptr;
+    if (plan->delta_nnz > 0)
+      k_delta_fill<<<wgrid, 256, 0, s>>>(words, M, Kw, plan->cons, plan->row_cluster,
+                                         plan->delta_ptr, plan->delta_idx);
+    if (n_list > 0)
+      k_cons_fill<<<(unsigned)ceil_div(ncl, 8), 256, 0, s>>>(plan->cons, ncl, Kw, plan->cons_ptr, plan->cons_idx);
     BSP_LAUNCHED();
   }
   BSP_CUDA(cudaStreamSynchronize(s));

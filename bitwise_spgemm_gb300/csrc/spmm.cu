@@ -14,8 +14,12 @@
 //   C[i] = P[c] + Σ_{k ∈ A_i \ cons_c} B[k] − Σ_{k ∈ cons_c \ A_i} B[k],
 // where P[c] = Σ_{k ∈ cons_c} B[k] is computed once per cluster by
 // k_proto_sums (K split across the warps of a CTA, fixed-order reduction).
+#include <cooperative_groups.h>
+
 #include "ptx.cuh"
 #include "spmm_dev.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace bsp {
 namespace {
@@ -200,6 +204,83 @@ __global__ void __launch_bounds__(512) k_proto_sums(SpmmArgs a) {
   }
 }
 
+// P[c] over one chunk of CW = 32·VPL·COLS columns from the prototype's
+// column list, by a cluster of 8 CTAs × 8 warps: warp p = rank·8 + w sums
+// list entries [len·p/64, len·(p+1)/64) with one B slice in flight.  With 64
+// short chains instead of 16 long ones the sums finish sooner (each gather
+// waits out the L2 latency of a loaded GPU), and 256-thread CTAs at 32
+// registers leave the SMs to the row kernel that runs beside them under
+// programmatic dependent launch.  Each CTA adds its warps' partials in warp
+// order; rank 0 adds the 8 CTA partials in rank order through distributed
+// shared memory (all loads issued first), so P is the same on every run.
+constexpr int kSumCluster = 8;
+template <typename BT, int VPL, bool OFF32>
+__global__ void __cluster_dims__(kSumCluster, 1, 1) __launch_bounds__(256) k_proto_sums_list(SpmmArgs a) {
+  using V = Vec<BT>;
+  constexpr int COLS = V::COLS;
+  constexpr int CW = 32 * VPL * COLS;
+  constexpr int PARTS = kSumCluster * 8;
+  __shared__ float4 wp[8][CW / 4];
+  __shared__ float4 cp[CW / 4];
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int n0 = (int)(blockIdx.x / kSumCluster) * CW;
+  const int64_t c = blockIdx.y;
+  ptx::griddep_launch_dependents();
+  int col[VPL];
+  bool cvalid[VPL];
+#pragma unroll
+  for (int v = 0; v < VPL; v++) {
+    col[v] = n0 + (v * 32 + lane) * COLS;
+    cvalid[v] = col[v] < (int)a.N;
+  }
+  const int s0 = __ldg(a.cons_ptr + c), len = __ldg(a.cons_ptr + c + 1) - s0;
+  const int p = rank * 8 + wid;
+  ListWalker wk;
+  wk.init(a.cons_idx, s0 + (int)((int64_t)len * p / PARTS), s0 + (int)((int64_t)len * (p + 1) / PARTS), lane);
+  Acc<VPL, COLS, false> acc;
+  acc.zero();
+  const BT* __restrict__ B = static_cast<const BT*>(a.B);
+  if (OFF32) accumulate_walk<BT, VPL, 1, false>(wk, B, (uint32_t)a.ldb, col, cvalid, acc);
+  else accumulate_walk<BT, VPL, 1, false>(wk, B, a.ldb, col, cvalid, acc);
+  float* w = reinterpret_cast<float*>(&wp[wid][0]);
+#pragma unroll
+  for (int v = 0; v < VPL; v++)
+#pragma unroll
+    for (int j = 0; j < COLS; j++) w[(v * 32 + lane) * COLS + j] = acc.result(v, j);
+  __syncthreads();
+  if (threadIdx.x < CW / 4) {
+    float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+      const float4 x = wp[u][threadIdx.x];
+      t.x += x.x;
+      t.y += x.y;
+      t.z += x.z;
+      t.w += x.w;
+    }
+    cp[threadIdx.x] = t;
+  }
+  cluster.sync();
+  if (rank == 0 && threadIdx.x < CW / 4) {
+    float4 x[kSumCluster];
+#pragma unroll
+    for (int r = 0; r < kSumCluster; r++) x[r] = cluster.map_shared_rank(cp, r)[threadIdx.x];
+    float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int r = 0; r < kSumCluster; r++) {
+      t.x += x[r].x;
+      t.y += x[r].y;
+      t.z += x[r].z;
+      t.w += x[r].w;
+    }
+    // P rows are ldp = ceil8(N) floats: a float4 starting below N stays in the row
+    if (n0 + 4 * (int)threadIdx.x < (int)a.N) reinterpret_cast<float4*>(a.P + c * a.ldp + n0)[threadIdx.x] = t;
+  }
+  cluster.sync();
+}
+
 template <typename BT>
 int launch_rows_t(const SpmmArgs& a, bool proto, bool vec, cudaStream_t s) {
   constexpr int COLS = Vec<BT>::COLS;
@@ -273,9 +354,18 @@ int launch_proto_regs_v(const SpmmArgs& a, int variant, cudaStream_t s) {
 
 template <typename BT>
 int launch_proto_t(const SpmmArgs& a, cudaStream_t s) {
+  constexpr int VPL = Vec<BT>::COLS == 4 ? 2 : 1;
+  constexpr int CWL = 32 * VPL * Vec<BT>::COLS;
+  const bool comp = a.proto_max_nnz > kCompThreshold;
+  if (a.cons_idx && !comp && a.n_proto <= 65535 && ceil_div(a.N, CWL) * kSumCluster <= 0x7fffffff) {
+    const dim3 g((unsigned)(ceil_div(a.N, CWL) * kSumCluster), (unsigned)a.n_proto);
+    if (a.K * a.ldb < ((int64_t)1 << 31)) k_proto_sums_list<BT, VPL, true><<<g, 256, 0, s>>>(a);
+    else k_proto_sums_list<BT, VPL, false><<<g, 256, 0, s>>>(a);
+    BSP_LAUNCHED();
+    return BSP_OK;
+  }
   constexpr int CW = 32 * Vec<BT>::COLS;
   const int threads = 512;
-  const bool comp = a.proto_max_nnz > kCompThreshold;
   const size_t smem = (size_t)(threads / 32) * CW * sizeof(float) * (comp ? 2 : 1);
   const dim3 g((unsigned)a.n_proto, (unsigned)ceil_div(a.N, CW));
   const bool off32 = a.K * a.ldb < ((int64_t)1 << 31);

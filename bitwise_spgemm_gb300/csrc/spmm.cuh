@@ -45,6 +45,8 @@ struct SpmmArgs {
   const uint32_t* cons;        // [n_proto][Kw] prototype masks
   int64_t n_proto;
   int64_t proto_max_nnz;       // set bits of the densest prototype (TwoSum above 4096)
+  const int32_t* cons_ptr;     // [n_proto + 1] prototype column lists, or null
+  const uint32_t* cons_idx;
   float* P;                    // [n_proto][ldp] prototype sums (workspace)
   int64_t ldp;
   // optional row subset for the walking kernel (rows of A without a cluster)
