@@ -515,6 +515,21 @@ __global__ void __launch_bounds__(256) k_finalize_rows(
 }
 
 
+// Warp per row: word 0 of the row's 128-byte slot is its delta count (0 for
+// rows without a cluster), words 1..31 its first 31 delta entries, so the
+// SpMM reads a row's list with one load whose address depends on the row
+// alone.
+__global__ void __launch_bounds__(256) k_delta_pad(const int32_t* __restrict__ cluster, int64_t M,
+                                                   const int32_t* __restrict__ dptr,
+                                                   const uint32_t* __restrict__ didx, uint32_t* __restrict__ pad) {
+  const int lane = threadIdx.x & 31;
+  const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  if (row >= M) return;
+  const int s = dptr[row];
+  const int n = cluster[row] >= 0 ? dptr[row + 1] - s : 0;
+  pad[row * 32 + lane] = lane == 0 ? (uint32_t)n : (lane - 1 < n ? didx[s + lane - 1] : 0u);
+}
+
 // Warp per prototype: its set columns in ascending order into
 // cons_idx[cons_ptr[c] ..] (the list the prototype-sum kernel walks).
 __global__ void __launch_bounds__(256) k_cons_fill(const uint32_t* __restrict__ cons, int64_t n_proto, int Kw,
@@ -987,15 +1002,20 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
   }
   // the prototypes' column lists (int32 offsets: kept only below 2^31 entries)
   const int64_t n_list = plan->proto_nnz < INT_MAX ? plan->proto_nnz : 0;
+  // each row's first 31 delta entries in a 128-byte slot (up to 1 GiB of slots)
+  const int64_t n_pad = M * 128 <= ((int64_t)1 << 30) ? M * 32 : 0;
   if (mode == BSP_PLAN_PROTO && plan->delta_nnz + n_list > 0) {
-    // one block: the delta lists, then the prototypes' column lists
-    BSP_CUDA(plan_alloc(&plan->delta_arena, sizeof(uint32_t) * (plan->delta_nnz + n_list), s,
+    // one block: the row slots, the delta lists, then the prototypes' column lists
+    BSP_CUDA(plan_alloc(&plan->delta_arena, sizeof(uint32_t) * (n_pad + plan->delta_nnz + n_list), s,
                         &plan->delta_pooled));
-    plan->delta_idx = (uint32_t*)plan->delta_arena;
+    plan->delta_pad = n_pad > 0 ? (uint32_t*)plan->delta_arena : nullptr;
+    plan->delta_idx = (uint32_t*)plan->delta_arena + n_pad;
     plan->cons_idx = n_list > 0 ? plan->delta_idx + plan->delta_nnz : nullptr;
     if (plan->delta_nnz > 0)
       k_delta_fill<<<wgrid, 256, 0, s>>>(words, M, Kw, plan->cons, plan->row_cluster,
                                          plan->delta_ptr, plan->delta_idx);
+    if (n_pad > 0)
+      k_delta_pad<<<wgrid, 256, 0, s>>>(plan->row_cluster, M, plan->delta_ptr, plan->delta_idx, plan->delta_pad);
     if (n_list > 0)
       k_cons_fill<<<(unsigned)ceil_div(ncl, 8), 256, 0, s>>>(plan->cons, ncl, Kw, plan->cons_ptr, plan->cons_idx);
     BSP_LAUNCHED();

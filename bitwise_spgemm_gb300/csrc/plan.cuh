@@ -17,6 +17,7 @@ struct bsp_plan {
   int32_t* delta_ptr = nullptr;
   uint32_t* delta_idx = nullptr;
   uint32_t* cons = nullptr;
+  uint32_t* delta_pad = nullptr;   // [M][32]: count, then the first 31 delta entries (or null)
   int32_t* cons_ptr = nullptr;     // [n_proto + 1]: each prototype's columns in cons_idx
   uint32_t* cons_idx = nullptr;    // prototype columns, ascending per prototype (proto plans)
   int32_t* direct_list = nullptr;  // rows without a cluster (ascending), direct_rows entries

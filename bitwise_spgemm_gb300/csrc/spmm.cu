@@ -96,13 +96,16 @@ __global__ void __launch_bounds__(256) k_spmm_rows(SpmmArgs a) {
 // arithmetic (M < 2^31, checked on the host) they keep the 8-blocks-per-SM
 // shape within its 32 registers without spilling (a 12-byte spill cost the
 // clustered 8192²×512 step 3 µs).
-template <typename BT, int VPL, int D, int MINB, bool OFF32, bool FULL>
+template <typename BT, int VPL, int D, int MINB, bool OFF32, bool FULL, bool SLOT>
 __global__ void __launch_bounds__(256, MINB) k_spmm_proto_regs(SpmmArgs a) {
   using V = Vec<BT>;
   constexpr int COLS = V::COLS;
   constexpr int CW = 32 * VPL * COLS;
   const int lane = threadIdx.x & 31;
   const int row = (int)blockIdx.x * 8 + (threadIdx.x >> 5);
+  // SLOT: the row's list comes from its 128-byte slot, loaded beside the
+  // cluster id (one load latency before the gathers instead of two)
+  const uint32_t slot = (SLOT && row < (int)a.M) ? __ldg(a.delta_pad + (int64_t)row * 32 + lane) : 0u;
   const int cl = row < (int)a.M ? __ldg(a.row_cluster + row) : -1;
   if (cl >= 0) {
     const int n0 = (int)blockIdx.y * CW;
@@ -114,12 +117,19 @@ __global__ void __launch_bounds__(256, MINB) k_spmm_proto_regs(SpmmArgs a) {
       col[v] = n0 + (v * 32 + lane) * COLS;
       cvalid[v] = FULL || col[v] < (int)a.N;
     }
-    ListWalker wk;
-    wk.init(a.delta_idx, __ldg(a.delta_ptr + row), __ldg(a.delta_ptr + row + 1), lane);
     Acc<VPL, COLS, false> acc;
     acc.zero();
-    if (OFF32) accumulate_walk<BT, VPL, D, false>(wk, B, (uint32_t)a.ldb, col, cvalid, acc);
-    else accumulate_walk<BT, VPL, D, false>(wk, B, a.ldb, col, cvalid, acc);
+    if (SLOT) {
+      SlotWalker wk;
+      wk.init(slot, a.delta_idx, a.delta_ptr, row, lane);
+      if (OFF32) accumulate_walk<BT, VPL, D, false>(wk, B, (uint32_t)a.ldb, col, cvalid, acc);
+      else accumulate_walk<BT, VPL, D, false>(wk, B, a.ldb, col, cvalid, acc);
+    } else {
+      ListWalker wk;
+      wk.init(a.delta_idx, __ldg(a.delta_ptr + row), __ldg(a.delta_ptr + row + 1), lane);
+      if (OFF32) accumulate_walk<BT, VPL, D, false>(wk, B, (uint32_t)a.ldb, col, cvalid, acc);
+      else accumulate_walk<BT, VPL, D, false>(wk, B, a.ldb, col, cvalid, acc);
+    }
     ptx::griddep_wait();
     store_vecs<VPL, COLS, false>(a.C + (int64_t)row * a.ldc, col, cvalid, acc, a.P + (int64_t)cl * a.ldp);
   } else {
@@ -313,6 +323,15 @@ int launch_rows_t(const SpmmArgs& a, bool proto, bool vec, cudaStream_t s) {
   return BSP_OK;
 }
 
+// BSP_SLOT_LISTS=0 reads every row's list through its bounds (for comparisons).
+bool slot_lists_enabled() {
+  static const bool on = [] {
+    const char* e = getenv("BSP_SLOT_LISTS");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
 template <typename BT, int VPL, int D, int MINB>
 int launch_proto_regs_t(const SpmmArgs& a, cudaStream_t s) {
   constexpr int CW = 32 * VPL * Vec<BT>::COLS;
@@ -327,12 +346,14 @@ int launch_proto_regs_t(const SpmmArgs& a, cudaStream_t s) {
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   const bool off32 = a.K * a.ldb < ((int64_t)1 << 31), full = a.N % CW == 0;
-  if (off32 && full)
-    BSP_CUDA(cudaLaunchKernelEx(&cfg, k_spmm_proto_regs<BT, VPL, D, MINB, true, true>, a));
+  if (off32 && full && a.delta_pad && slot_lists_enabled())
+    BSP_CUDA(cudaLaunchKernelEx(&cfg, k_spmm_proto_regs<BT, VPL, D, MINB, true, true, true>, a));
+  else if (off32 && full)
+    BSP_CUDA(cudaLaunchKernelEx(&cfg, k_spmm_proto_regs<BT, VPL, D, MINB, true, true, false>, a));
   else if (off32)
-    BSP_CUDA(cudaLaunchKernelEx(&cfg, k_spmm_proto_regs<BT, VPL, D, MINB, true, false>, a));
+    BSP_CUDA(cudaLaunchKernelEx(&cfg, k_spmm_proto_regs<BT, VPL, D, MINB, true, false, false>, a));
   else
-    BSP_CUDA(cudaLaunchKernelEx(&cfg, k_spmm_proto_regs<BT, VPL, D, MINB, false, false>, a));
+    BSP_CUDA(cudaLaunchKernelEx(&cfg, k_spmm_proto_regs<BT, VPL, D, MINB, false, false, false>, a));
   return BSP_OK;
 }
 

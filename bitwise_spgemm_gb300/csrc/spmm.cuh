@@ -45,6 +45,7 @@ struct SpmmArgs {
   const uint32_t* cons;        // [n_proto][Kw] prototype masks
   int64_t n_proto;
   int64_t proto_max_nnz;       // set bits of the densest prototype (TwoSum above 4096)
+  const uint32_t* delta_pad;   // [M][32] count + first 31 delta entries per row, or null
   const int32_t* cons_ptr;     // [n_proto + 1] prototype column lists, or null
   const uint32_t* cons_idx;
   float* P;                    // [n_proto][ldp] prototype sums (workspace)

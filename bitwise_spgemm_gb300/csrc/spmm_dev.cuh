@@ -111,6 +111,29 @@ struct ListWalker {
   }
 };
 
+// A row's delta list from its 128-byte slot (word 0 = count, words 1..31 =
+// the first 31 entries, one per lane) and, past 31 entries, from the list:
+// the same entries in the same order as a ListWalker over the whole list.
+struct SlotWalker {
+  uint32_t slot;
+  int n, j;
+  ListWalker tail;
+  __device__ void init(uint32_t slot_, const uint32_t* list, const int32_t* dptr, int64_t row, int lane) {
+    slot = slot_;
+    n = (int)__shfl_sync(kFull, slot_, 0);
+    j = 0;
+    const int s = n > 31 ? __ldg(dptr + row) : 0;
+    tail.init(list, s + 31, n > 31 ? s + n : s + 31, lane);
+  }
+  __device__ __forceinline__ uint32_t next() {
+    if (j < n && j < 31) {
+      j++;
+      return __shfl_sync(kFull, slot, j);
+    }
+    return tail.next();
+  }
+};
+
 template <int VPL, int COLS, bool COMP>
 struct Acc {
   float s[VPL][COLS];

@@ -255,6 +255,47 @@ def test_proto_bulk_mixed_rows(N, bdt):
     assert capi.device_status() == 0
 
 
+@pytest.mark.parametrize("N,bdt", [(512, "f32"), (256, "f32"), (512, "bf16")])
+def test_proto_delta_lists_across_the_row_slot(N, bdt):
+    """Rows that differ from their prototype in exactly f columns, f from 0 to
+    100: the row kernel reads the first 31 delta entries from the row's slot
+    and the rest from the list, so counts 30..33 and 62..64 cross both edges.
+    Integer-valued B is exact; Gaussian B within the FP32 bound."""
+    rng = np.random.default_rng(N + 7)
+    K, flips = 4096, [0, 1, 2, 30, 31, 32, 33, 62, 63, 64, 100]
+    protos = rng.random((4, K)) < 0.1
+    rows = []
+    for p in protos:
+        for f in flips:
+            for _ in range(6):
+                r = p.copy()
+                idx = rng.choice(K, f, replace=False)
+                r[idx] = ~r[idx]
+                rows.append(r)
+    A = np.array(rows)
+    words = W.pack_bits(A)
+    wd = words_dev(words)
+    plan = ops.Plan(wd, K, mode=capi.PLAN_PROTO)
+    info = plan.info()
+    assert info["mode"] == capi.PLAN_PROTO and info["delta_nnz"] > 0
+    Bi = rng.integers(-8, 9, (K, N)).astype(np.float32)
+    if bdt == "bf16":
+        Bd = bf16_dev(W.f32_to_bf16_bits(Bi))
+    else:
+        Bd = torch.from_numpy(Bi).cuda()
+    Ci = ops.spmm(wd, K, Bd, plan=plan).cpu().numpy()
+    assert capi.device_status() == 0
+    assert np.array_equal(Ci.astype(np.float64), O.spmm_f64(words, K, Bi))
+    Bf = rng.standard_normal((K, N)).astype(np.float32)
+    if bdt == "bf16":
+        b16 = W.f32_to_bf16_bits(Bf)
+        Bf, Bd = W.bf16_bits_to_f32(b16), bf16_dev(b16)
+    else:
+        Bd = torch.from_numpy(Bf).cuda()
+    C = ops.spmm(wd, K, Bd, plan=plan).cpu().numpy()
+    _check_f64(C, words, K, Bf)
+
+
 def test_plan_destroy_async_in_a_loop():
     """Plans built, used and released in stream order, back to back on one
     stream without a host wait between steps (the serving-loop pattern):
