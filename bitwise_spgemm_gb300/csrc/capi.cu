@@ -253,10 +253,14 @@ static int proto_path() {  // 0 = register gathers (default), 1 = TMA-staged sli
   }
   return v;
 }
-static int proto_variant() {
+// Register gathers: one 1 KB half row per warp with one gather in flight
+// (variant 4) for FP32 B; 16-bit B keeps 512 columns per warp and two gathers
+// in flight (variant 0), 22.4 against 27.1 us at 8192x8192x512 BF16.
+static int proto_variant(int esz) {
   static int v = -1000;
-  if (v == -1000) v = env_int("BSP_PROTO_VARIANT", proto_path() == 1 ? 3 : 4);
-  return v;
+  if (v == -1000) v = env_int("BSP_PROTO_VARIANT", -1);
+  if (v >= 0) return v;
+  return proto_path() == 1 ? 3 : esz == 4 ? 4 : 0;
 }
 
 // Default schedule: the cost model for the engine (BSP_TC=0/1 forces it),
@@ -266,7 +270,7 @@ static TuneSched default_schedule(const bsp_plan* plan, int64_t N, int esz, bool
   TuneSched t;
   t.engine = (tc_ok && use_tensor_cores(plan, N, esz)) ? 1 : 2;
   t.proto_path = proto_path();
-  t.proto_variant = proto_variant();
+  t.proto_variant = proto_variant(esz);
   return t;
 }
 
@@ -422,7 +426,7 @@ int bsp_tune(const uint32_t* A_words, int64_t M, int64_t K, const void* B, int b
     for (int v = 0; v <= 6; v++) cand[nc++] = TuneSched{2, 0, v, 0.0};
     for (int v = 0; v <= 7; v++) cand[nc++] = TuneSched{2, 1, v, 0.0};
   } else {
-    cand[nc++] = TuneSched{2, 0, proto_variant(), 0.0};
+    cand[nc++] = TuneSched{2, 0, proto_variant(esz), 0.0};
   }
   cudaEvent_t e0, e1;
   BSP_CUDA(cudaEventCreate(&e0));
