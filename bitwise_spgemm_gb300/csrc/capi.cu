@@ -296,6 +296,7 @@ static int run_spmm(SpmmArgs a, const bsp_plan* plan, bool vec, const TuneSched&
     a.proto_max_nnz = plan->proto_max_nnz;
     a.cons_ptr = plan->cons_ptr;
     a.delta_pad = plan->delta_pad;
+    a.n_slot = plan->n_slot;
     a.cons_idx = plan->cons_idx;
     a.P = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255));
     a.ldp = proto_ldp(N);

@@ -515,19 +515,71 @@ __global__ void __launch_bounds__(256) k_finalize_rows(
 }
 
 
-// Warp per row: word 0 of the row's 128-byte slot is its delta count (0 for
-// rows without a cluster), words 1..31 its first 31 delta entries, so the
-// SpMM reads a row's list with one load whose address depends on the row
-// alone.
-__global__ void __launch_bounds__(256) k_delta_pad(const int32_t* __restrict__ cluster, int64_t M,
-                                                   const int32_t* __restrict__ dptr,
-                                                   const uint32_t* __restrict__ didx, uint32_t* __restrict__ pad) {
+// ---- row slots: clustered rows by descending delta count -----------------
+// The SpMM's warps take clustered rows in slot order, and the GPU starts CTAs
+// in index order, so the longest lists start first and the last CTAs to
+// start carry the shortest ones (a shorter tail).  A stable counting sort on
+// min(count, 255): per-block bucket counts, one scan over (bucket
+// descending, block), then each row's rank among the same bucket's earlier
+// rows in its block.
+constexpr int kOrderBuckets = 256;
+__device__ __forceinline__ int order_bucket(const int32_t* cluster, const int32_t* dptr, int64_t row, int64_t M) {
+  if (row >= M || cluster[row] < 0) return -1;
+  const int n = dptr[row + 1] - dptr[row];
+  return n < kOrderBuckets - 1 ? n : kOrderBuckets - 1;
+}
+
+__global__ void __launch_bounds__(256) k_order_count(const int32_t* __restrict__ cluster,
+                                                     const int32_t* __restrict__ dptr, int64_t M, int64_t nb,
+                                                     int32_t* __restrict__ cnt) {
+  __shared__ int h[kOrderBuckets];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const int b = order_bucket(cluster, dptr, (int64_t)blockIdx.x * 256 + threadIdx.x, M);
+  if (b >= 0) atomicAdd(&h[b], 1);
+  __syncthreads();
+  cnt[(int64_t)(kOrderBuckets - 1 - threadIdx.x) * nb + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(256) k_order_scatter(const int32_t* __restrict__ cluster,
+                                                       const int32_t* __restrict__ dptr, int64_t M, int64_t nb,
+                                                       const int32_t* __restrict__ base, int32_t* __restrict__ order) {
+  __shared__ int wc[8][kOrderBuckets];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < 8 * kOrderBuckets; i += 256) (&wc[0][0])[i] = 0;
+  __syncthreads();
+  const int64_t row = (int64_t)blockIdx.x * 256 + threadIdx.x;
+  const int b = order_bucket(cluster, dptr, row, M);
+  const unsigned peers = __match_any_sync(0xffffffffu, b);
+  const int rank = __popc(peers & ((1u << lane) - 1u));
+  if (b >= 0 && rank == 0) wc[w][b] = __popc(peers);
+  __syncthreads();
+  if (b < 0) return;
+  int before = rank;
+  for (int u = 0; u < w; u++) before += wc[u][b];
+  order[base[(int64_t)(kOrderBuckets - 1 - b) * nb + blockIdx.x] + before] = (int32_t)row;
+}
+
+// Warp per slot p: the 128-byte slot of row order[p] holds the row, its
+// cluster, its delta count, the list's start and the first 28 entries, so
+// the SpMM reads a row's whole description with one load whose address
+// depends on p alone.
+__global__ void __launch_bounds__(256) k_delta_slots(const int32_t* __restrict__ order, int64_t n_slot,
+                                                     const int32_t* __restrict__ cluster,
+                                                     const int32_t* __restrict__ dptr,
+                                                     const uint32_t* __restrict__ didx, uint32_t* __restrict__ pad) {
   const int lane = threadIdx.x & 31;
-  const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  if (row >= M) return;
-  const int s = dptr[row];
-  const int n = cluster[row] >= 0 ? dptr[row + 1] - s : 0;
-  pad[row * 32 + lane] = lane == 0 ? (uint32_t)n : (lane - 1 < n ? didx[s + lane - 1] : 0u);
+  const int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  if (p >= n_slot) return;
+  const int row = order[p];
+  const int s = dptr[row], n = dptr[row + 1] - s;
+  uint32_t v;
+  if (lane == 0) v = (uint32_t)row;
+  else if (lane == 1) v = (uint32_t)cluster[row];
+  else if (lane == 2) v = (uint32_t)n;
+  else if (lane == 3) v = (uint32_t)s;
+  else v = lane - 4 < n ? didx[s + lane - 4] : 0u;
+  pad[p * 32 + lane] = v;
 }
 
 // Warp per prototype: its set columns in ascending order into
@@ -847,7 +899,7 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
   const size_t o_flag = take(sizeof(int32_t) * M);
   const size_t o_cid = take(sizeof(int32_t) * (M + 1));
   const size_t o_coff = take(sizeof(int32_t) * (M + 1));
-  const size_t o_scan = take(scan_workspace_bytes(M + 1));
+  const size_t o_scan = take(scan_workspace_bytes(M + kOrderBuckets + 1));
   const size_t o_stats = take(sizeof(unsigned long long) * 8);
   const size_t o_dcnt = take(sizeof(int32_t) * M);
   DevBuf tmp;
@@ -1002,8 +1054,9 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
   }
   // the prototypes' column lists (int32 offsets: kept only below 2^31 entries)
   const int64_t n_list = plan->proto_nnz < INT_MAX ? plan->proto_nnz : 0;
-  // each row's first 31 delta entries in a 128-byte slot (up to 1 GiB of slots)
-  const int64_t n_pad = M * 128 <= ((int64_t)1 << 30) ? M * 32 : 0;
+  // a 128-byte slot per clustered row (up to 1 GiB of slots)
+  const int64_t n_slot = M - plan->direct_rows;
+  const int64_t n_pad = n_slot > 0 && n_slot * 128 <= ((int64_t)1 << 30) ? n_slot * 32 : 0;
   if (mode == BSP_PLAN_PROTO && plan->delta_nnz + n_list > 0) {
     // one block: the row slots, the delta lists, then the prototypes' column lists
     BSP_CUDA(plan_alloc(&plan->delta_arena, sizeof(uint32_t) * (n_pad + plan->delta_nnz + n_list), s,
@@ -1014,8 +1067,22 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
     if (plan->delta_nnz > 0)
       k_delta_fill<<<wgrid, 256, 0, s>>>(words, M, Kw, plan->cons, plan->row_cluster,
                                          plan->delta_ptr, plan->delta_idx);
-    if (n_pad > 0)
-      k_delta_pad<<<wgrid, 256, 0, s>>>(plan->row_cluster, M, plan->delta_ptr, plan->delta_idx, plan->delta_pad);
+    if (n_pad > 0) {
+      const int64_t nb = ceil_div(M, 256), nc = kOrderBuckets * nb;
+      DevBuf ob;
+      BSP_TRY(ob.alloc(sizeof(int32_t) * (size_t)(n_slot + 2 * nc + 1), s));
+      int32_t* order = static_cast<int32_t*>(ob.p);
+      int32_t* cnt = order + n_slot;
+      int32_t* base = cnt + nc;
+      k_order_count<<<(unsigned)nb, 256, 0, s>>>(plan->row_cluster, plan->delta_ptr, M, nb, cnt);
+      BSP_LAUNCHED();
+      BSP_TRY(launch_scan_i32(cnt, nc, base, scanws, s));
+      k_order_scatter<<<(unsigned)nb, 256, 0, s>>>(plan->row_cluster, plan->delta_ptr, M, nb, base, order);
+      k_delta_slots<<<(unsigned)ceil_div(n_slot, 8), 256, 0, s>>>(order, n_slot, plan->row_cluster,
+                                                                   plan->delta_ptr, plan->delta_idx, plan->delta_pad);
+      BSP_LAUNCHED();
+      plan->n_slot = n_slot;
+    }
     if (n_list > 0)
       k_cons_fill<<<(unsigned)ceil_div(ncl, 8), 256, 0, s>>>(plan->cons, ncl, Kw, plan->cons_ptr, plan->cons_idx);
     BSP_LAUNCHED();

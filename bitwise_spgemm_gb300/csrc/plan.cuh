@@ -17,7 +17,8 @@ struct bsp_plan {
   int32_t* delta_ptr = nullptr;
   uint32_t* delta_idx = nullptr;
   uint32_t* cons = nullptr;
-  uint32_t* delta_pad = nullptr;   // [M][32]: count, then the first 31 delta entries (or null)
+  uint32_t* delta_pad = nullptr;   // [n_slot][32] row slots by descending delta count (or null)
+  int64_t n_slot = 0;              // clustered rows with a slot
   int32_t* cons_ptr = nullptr;     // [n_proto + 1]: each prototype's columns in cons_idx
   uint32_t* cons_idx = nullptr;    // prototype columns, ascending per prototype (proto plans)
   int32_t* direct_list = nullptr;  // rows without a cluster (ascending), direct_rows entries

@@ -102,11 +102,19 @@ __global__ void __launch_bounds__(256, MINB) k_spmm_proto_regs(SpmmArgs a) {
   constexpr int COLS = V::COLS;
   constexpr int CW = 32 * VPL * COLS;
   const int lane = threadIdx.x & 31;
-  const int row = (int)blockIdx.x * 8 + (threadIdx.x >> 5);
-  // SLOT: the row's list comes from its 128-byte slot, loaded beside the
-  // cluster id (one load latency before the gathers instead of two)
-  const uint32_t slot = (SLOT && row < (int)a.M) ? __ldg(a.delta_pad + (int64_t)row * 32 + lane) : 0u;
-  const int cl = row < (int)a.M ? __ldg(a.row_cluster + row) : -1;
+  int row, cl;
+  uint32_t slot = 0u;
+  if (SLOT) {
+    // warp p takes the p-th row slot (rows by descending delta count): row,
+    // cluster and list in one load whose address depends on p alone
+    const int p = (int)blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (p < (int)a.n_slot) slot = __ldg(a.delta_pad + (int64_t)p * 32 + lane);
+    row = (int)__shfl_sync(kFull, slot, 0);
+    cl = p < (int)a.n_slot ? (int)__shfl_sync(kFull, slot, 1) : -1;
+  } else {
+    row = (int)blockIdx.x * 8 + (threadIdx.x >> 5);
+    cl = row < (int)a.M ? __ldg(a.row_cluster + row) : -1;
+  }
   if (cl >= 0) {
     const int n0 = (int)blockIdx.y * CW;
     const BT* __restrict__ B = static_cast<const BT*>(a.B);
@@ -121,7 +129,7 @@ __global__ void __launch_bounds__(256, MINB) k_spmm_proto_regs(SpmmArgs a) {
     acc.zero();
     if (SLOT) {
       SlotWalker wk;
-      wk.init(slot, a.delta_idx, a.delta_ptr, row, lane);
+      wk.init(slot, a.delta_idx, lane);
       if (OFF32) accumulate_walk<BT, VPL, D, false>(wk, B, (uint32_t)a.ldb, col, cvalid, acc);
       else accumulate_walk<BT, VPL, D, false>(wk, B, a.ldb, col, cvalid, acc);
     } else {
@@ -323,7 +331,8 @@ int launch_rows_t(const SpmmArgs& a, bool proto, bool vec, cudaStream_t s) {
   return BSP_OK;
 }
 
-// BSP_SLOT_LISTS=0 reads every row's list through its bounds (for comparisons).
+// BSP_SLOT_LISTS=0: rows in index order, each list read through its bounds
+// (for comparisons).
 bool slot_lists_enabled() {
   static const bool on = [] {
     const char* e = getenv("BSP_SLOT_LISTS");
@@ -336,7 +345,9 @@ template <typename BT, int VPL, int D, int MINB>
 int launch_proto_regs_t(const SpmmArgs& a, cudaStream_t s) {
   constexpr int CW = 32 * VPL * Vec<BT>::COLS;
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)ceil_div(a.M, 8), (unsigned)ceil_div(a.N, CW));
+  const bool off32 = a.K * a.ldb < ((int64_t)1 << 31), full = a.N % CW == 0;
+  const bool slot = off32 && full && a.delta_pad && a.n_slot > 0 && slot_lists_enabled();
+  cfg.gridDim = dim3((unsigned)ceil_div(slot ? a.n_slot : a.M, 8), (unsigned)ceil_div(a.N, CW));
   cfg.blockDim = dim3(256);
   cfg.dynamicSmemBytes = 0;
   cfg.stream = s;
@@ -345,8 +356,7 @@ int launch_proto_regs_t(const SpmmArgs& a, cudaStream_t s) {
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  const bool off32 = a.K * a.ldb < ((int64_t)1 << 31), full = a.N % CW == 0;
-  if (off32 && full && a.delta_pad && slot_lists_enabled())
+  if (slot)
     BSP_CUDA(cudaLaunchKernelEx(&cfg, k_spmm_proto_regs<BT, VPL, D, MINB, true, true, true>, a));
   else if (off32 && full)
     BSP_CUDA(cudaLaunchKernelEx(&cfg, k_spmm_proto_regs<BT, VPL, D, MINB, true, true, false>, a));

@@ -45,7 +45,8 @@ struct SpmmArgs {
   const uint32_t* cons;        // [n_proto][Kw] prototype masks
   int64_t n_proto;
   int64_t proto_max_nnz;       // set bits of the densest prototype (TwoSum above 4096)
-  const uint32_t* delta_pad;   // [M][32] count + first 31 delta entries per row, or null
+  const uint32_t* delta_pad;   // [n_slot][32] row slots (row, cluster, count, start, 28 entries), or null
+  int64_t n_slot;              // clustered rows, in slot order
   const int32_t* cons_ptr;     // [n_proto + 1] prototype column lists, or null
   const uint32_t* cons_idx;
   float* P;                    // [n_proto][ldp] prototype sums (workspace)

@@ -111,25 +111,24 @@ struct ListWalker {
   }
 };
 
-// A row's delta list from its 128-byte slot (word 0 = count, words 1..31 =
-// the first 31 entries, one per lane) and, past 31 entries, from the list:
-// the same entries in the same order as a ListWalker over the whole list.
+// A row's delta list from its 128-byte slot (words 2 and 3 = count and the
+// list's start, words 4..31 = the first 28 entries, one per lane) and, past
+// 28 entries, from the list: the same entries in the same order as a
+// ListWalker over the whole list.
 struct SlotWalker {
+  static constexpr int kIn = 28;
   uint32_t slot;
   int n, j;
   ListWalker tail;
-  __device__ void init(uint32_t slot_, const uint32_t* list, const int32_t* dptr, int64_t row, int lane) {
+  __device__ void init(uint32_t slot_, const uint32_t* list, int lane) {
     slot = slot_;
-    n = (int)__shfl_sync(kFull, slot_, 0);
+    n = (int)__shfl_sync(kFull, slot_, 2);
+    const int s = (int)__shfl_sync(kFull, slot_, 3);
     j = 0;
-    const int s = n > 31 ? __ldg(dptr + row) : 0;
-    tail.init(list, s + 31, n > 31 ? s + n : s + 31, lane);
+    tail.init(list, s + kIn, n > kIn ? s + n : s + kIn, lane);
   }
   __device__ __forceinline__ uint32_t next() {
-    if (j < n && j < 31) {
-      j++;
-      return __shfl_sync(kFull, slot, j);
-    }
+    if (j < n && j < kIn) return __shfl_sync(kFull, slot, 4 + j++);
     return tail.next();
   }
 };
