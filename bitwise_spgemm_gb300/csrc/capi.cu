@@ -253,14 +253,15 @@ static int proto_path() {  // 0 = register gathers (default), 1 = TMA-staged sli
   }
   return v;
 }
-// Register gathers: one 1 KB half row per warp with one gather in flight
-// (variant 4) for FP32 B; 16-bit B keeps 512 columns per warp and two gathers
-// in flight (variant 0), 22.4 against 27.1 us at 8192x8192x512 BF16.
+// Register gathers: 512 columns per warp and two gathers in flight (variant
+// 0) for every B type — at 8192x8192x512 FP32 22.55 us a step against 22.9
+// for a 1 KB half row with one in flight (variant 4), BF16 16.9 against 25.1.
 static int proto_variant(int esz) {
   static int v = -1000;
   if (v == -1000) v = env_int("BSP_PROTO_VARIANT", -1);
+  (void)esz;
   if (v >= 0) return v;
-  return proto_path() == 1 ? 3 : esz == 4 ? 4 : 0;
+  return proto_path() == 1 ? 3 : 0;
 }
 
 // Default schedule: the cost model for the engine (BSP_TC=0/1 forces it),
@@ -410,7 +411,7 @@ int bsp_tune(const uint32_t* A_words, int64_t M, int64_t K, const void* B, int b
   // stage, B by boxes or pre-tiled, split-K by the rule or never); every
   // prototype-kernel shape on both CUDA-core paths; the plain walk when the
   // plan has no prototypes
-  TuneSched cand[8 + 7 + 8];
+  TuneSched cand[8 + 9 + 8];
   int nc = 0;
   if (tc_ok)
     for (int tps = 2; tps <= 3; tps++)
@@ -424,7 +425,7 @@ int bsp_tune(const uint32_t* A_words, int64_t M, int64_t K, const void* B, int b
           cand[nc++] = t;
         }
   if (plan->mode == BSP_PLAN_PROTO && vec) {
-    for (int v = 0; v <= 6; v++) cand[nc++] = TuneSched{2, 0, v, 0.0};
+    for (int v = 0; v <= 8; v++) cand[nc++] = TuneSched{2, 0, v, 0.0};
     for (int v = 0; v <= 7; v++) cand[nc++] = TuneSched{2, 1, v, 0.0};
   } else {
     cand[nc++] = TuneSched{2, 0, proto_variant(esz), 0.0};

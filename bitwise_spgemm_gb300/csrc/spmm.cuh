@@ -69,6 +69,9 @@ int launch_spmm_proto_regs(const SpmmArgs& a, int variant, cudaStream_t s);
 int launch_spmm_proto_bulk(const SpmmArgs& a, int variant, cudaStream_t s);
 // Device-side error word of the bulk kernels (0 = none); clear resets it.
 int bulk_device_error(int* out, bool clear);
+// Prototype sums from the column lists with B slices staged by bulk copies
+// (B 16-byte aligned, ldb·esize and N·esize multiples of 16).
+int launch_proto_sums_bulk(const SpmmArgs& a, int variant, cudaStream_t s);
 
 // Tensor-core path (spmm_tc.cu) for 16-bit B: occupancy bitmap of 32-column
 // K tiles per 128-row block ([ceil(M/128)][tc_occupancy_words(K)]), then the

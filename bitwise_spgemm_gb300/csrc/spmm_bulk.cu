@@ -231,6 +231,174 @@ __global__ void __launch_bounds__(WARPS * 32, 1) k_spmm_proto_bulk(SpmmArgs a, i
   if (acc_row >= 0) store();
 }
 
+// Prototype sums P[c] over one chunk of CW = 32·VPL·COLS columns by one CTA
+// of WARPS warps: warp w walks entries [len·w/WARPS, len·(w+1)/WARPS) of the
+// prototype's column list, keeping S stages of SLOTS B slices in flight as
+// bulk copies (the bytes in flight cost shared memory, not registers), and
+// adds them in list order; the warps' partials are added in warp order, so P
+// is the same on every run.  Few warps with deep copy queues finish the sums
+// in a few L2 round trips while leaving most warp slots and registers of the
+// SM to the row kernel under programmatic dependent launch.  A wait that
+// runs out records error 2 in g_bulk_error; the warp waits (bounded) for its
+// other stages and the CTA writes nothing.
+template <typename BT, int VPL, int WARPS, int S, int SLOTS>
+struct SumsBulkLayout {
+  static constexpr int kCW = 32 * VPL * Vec<BT>::COLS;
+  static constexpr int kSlot = kCW * (int)sizeof(BT);
+  static constexpr size_t kBuf = (size_t)WARPS * S * SLOTS * kSlot;
+  static constexpr size_t kTotal = kBuf + (size_t)WARPS * S * sizeof(uint64_t);
+};
+
+template <typename BT, int VPL, int WARPS, int S, int SLOTS>
+__global__ void __launch_bounds__(WARPS * 32, 1) k_proto_sums_bulk(SpmmArgs a) {
+  using V = Vec<BT>;
+  using L = SumsBulkLayout<BT, VPL, WARPS, S, SLOTS>;
+  constexpr int COLS = V::COLS;
+  constexpr int CW = L::kCW;
+  static_assert(SLOTS <= 32, "one lane per slot");
+  static_assert(CW / 4 <= WARPS * 32, "one thread per float4 of the chunk");
+  static_assert(L::kTotal + WARPS * CW * 4 <= 232448, "shared memory");
+  extern __shared__ __align__(1024) uint8_t smem[];
+  __shared__ float4 wp[WARPS][CW / 4];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  uint8_t* buf = smem + (size_t)warp * S * SLOTS * L::kSlot;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + L::kBuf) + warp * S;
+  ptx::griddep_launch_dependents();
+
+  const int n0 = (int)blockIdx.x * CW;
+  const int64_t c = blockIdx.y;
+  const int ncols = min(CW, (int)(a.N - n0));
+  const uint32_t bytes = (uint32_t)ncols * (uint32_t)sizeof(BT);
+  const BT* Bn = static_cast<const BT*>(a.B) + n0;
+  const int s0 = __ldg(a.cons_ptr + c), len = __ldg(a.cons_ptr + c + 1) - s0;
+  int e = s0 + (int)((int64_t)len * warp / WARPS);
+  const int e_end = s0 + (int)((int64_t)len * (warp + 1) / WARPS);
+  int col[VPL];
+  bool cvalid[VPL];
+#pragma unroll
+  for (int v = 0; v < VPL; v++) {
+    col[v] = (v * 32 + lane) * COLS;
+    cvalid[v] = col[v] < ncols;
+  }
+  if (lane == 0)
+    for (int s = 0; s < S; s++) ptx::mbar_init(&bars[s], 1);
+  ptx::fence_mbar_init();
+  __syncwarp();
+
+  auto fill = [&](int s) -> int {
+    const int n = min(SLOTS, e_end - e);
+    if (n <= 0) return 0;
+    if (lane == 0) ptx::mbar_arrive_expect_tx(&bars[s], (uint32_t)n * bytes);
+    __syncwarp();
+    if (lane < n) {
+      const uint32_t k = __ldg(a.cons_idx + e + lane);
+      ptx::bulk_g2s(buf + (size_t)(s * SLOTS + lane) * L::kSlot, Bn + (int64_t)k * a.ldb, bytes, &bars[s]);
+    }
+    e += n;
+    return n;
+  };
+
+  Acc<VPL, COLS, false> acc;
+  acc.zero();
+  int ns[S];
+#pragma unroll
+  for (int s = 0; s < S; s++) ns[s] = fill(s);
+  uint32_t phases = 0;
+  bool ok = true;
+  for (bool any = true; any && ok;) {
+    any = false;
+#pragma unroll
+    for (int s = 0; s < S; s++) {
+      const int n = ns[s];
+      if (n == 0 || !ok) continue;
+      any = true;
+      if (!ptx::mbar_wait(&bars[s], (phases >> s) & 1u)) {
+        if (lane == 0) atomicCAS(&g_bulk_error, 0, 2);
+#pragma unroll
+        for (int t = 0; t < S; t++)
+          if (t != s && ns[t] > 0) ptx::mbar_wait(&bars[t], (phases >> t) & 1u);
+        ok = false;
+        continue;
+      }
+      phases ^= 1u << s;
+      for (int j = 0; j < n; j++) {
+        const uint8_t* slot = buf + (size_t)(s * SLOTS + j) * L::kSlot;
+#pragma unroll
+        for (int v = 0; v < VPL; v++) {
+          if (!cvalid[v]) continue;
+          const typename V::Raw r = *reinterpret_cast<const typename V::Raw*>(slot + (size_t)col[v] * sizeof(BT));
+          float f[COLS];
+          V::cvt(r, f);
+#pragma unroll
+          for (int q = 0; q < COLS; q++) acc.add(v, q, f[q]);
+        }
+      }
+      __syncwarp();
+      ptx::fence_proxy_async_smem();
+      ns[s] = fill(s);
+    }
+  }
+  float* w = reinterpret_cast<float*>(&wp[warp][0]);
+#pragma unroll
+  for (int v = 0; v < VPL; v++)
+#pragma unroll
+    for (int j = 0; j < COLS; j++) w[(v * 32 + lane) * COLS + j] = acc.result(v, j);
+  const int good = __syncthreads_and(ok ? 1 : 0);
+  if (good && threadIdx.x < CW / 4 && 4 * (int)threadIdx.x < ncols) {
+    float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int u = 0; u < WARPS; u++) {
+      const float4 x = wp[u][threadIdx.x];
+      t.x += x.x;
+      t.y += x.y;
+      t.z += x.z;
+      t.w += x.w;
+    }
+    reinterpret_cast<float4*>(a.P + c * a.ldp + n0)[threadIdx.x] = t;
+  }
+}
+
+template <typename BT, int VPL, int WARPS, int S, int SLOTS>
+int launch_sums_bulk_t(const SpmmArgs& a, cudaStream_t st) {
+  using L = SumsBulkLayout<BT, VPL, WARPS, S, SLOTS>;
+  static bool configured[64] = {false};
+  int dev = 0;
+  BSP_CUDA(cudaGetDevice(&dev));
+  auto kern = k_proto_sums_bulk<BT, VPL, WARPS, S, SLOTS>;
+  if (dev < 64 && !configured[dev]) {
+    BSP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::kTotal));
+    configured[dev] = true;
+  }
+  const int64_t chunks = ceil_div(a.N, L::kCW);
+  if (chunks > 0x7fffffff || a.n_proto > 65535) return BSP_ERR_CAPACITY;
+  kern<<<dim3((unsigned)chunks, (unsigned)a.n_proto), WARPS * 32, L::kTotal, st>>>(a);
+  BSP_LAUNCHED();
+  return BSP_OK;
+}
+
+template <typename BT, int VPL, int WARPS, int S, int SLOTS>
+int launch_sums_bulk_fit(const SpmmArgs& a, cudaStream_t st) {
+  using L = SumsBulkLayout<BT, VPL, WARPS, S, SLOTS>;
+  if constexpr (L::kTotal + (size_t)WARPS * L::kCW * 4 <= 232448) return launch_sums_bulk_t<BT, VPL, WARPS, S, SLOTS>(a, st);
+  else return BSP_ERR_UNSUPPORTED;
+}
+
+template <typename BT>
+int launch_sums_bulk_v(const SpmmArgs& a, int variant, cudaStream_t st) {
+  constexpr int VPL = Vec<BT>::COLS == 4 ? 2 : 1;
+  switch (variant) {
+    case 1: return launch_sums_bulk_fit<BT, VPL, 8, 2, 12>(a, st);
+    case 2: return launch_sums_bulk_fit<BT, VPL, 12, 2, 8>(a, st);
+    case 3: return launch_sums_bulk_fit<BT, VPL, 16, 2, 6>(a, st);
+    case 4: return launch_sums_bulk_fit<BT, VPL, 16, 3, 4>(a, st);
+    case 5: return launch_sums_bulk_fit<BT, VPL, 6, 2, 16>(a, st);
+    case 6: return launch_sums_bulk_fit<BT, VPL, 8, 3, 16>(a, st);
+    case 7: return launch_sums_bulk_fit<BT, VPL, 16, 2, 12>(a, st);
+    case 8: return launch_sums_bulk_fit<BT, VPL, 12, 2, 16>(a, st);
+    default: return launch_sums_bulk_fit<BT, VPL, 8, 3, 8>(a, st);
+  }
+}
+
 template <typename BT, int WARPS, int S, int SLOTS>
 int launch_bulk_t(const SpmmArgs& a, int n_delta, cudaStream_t st) {
   using L = BulkLayout<WARPS, S, SLOTS>;
@@ -275,6 +443,16 @@ int launch_spmm_proto_bulk(const SpmmArgs& a, int variant, cudaStream_t s) {
     case BSP_F32: return launch_bulk_variant<float>(a, n_delta, variant, s);
     case BSP_BF16: return launch_bulk_variant<__nv_bfloat16>(a, n_delta, variant, s);
     case BSP_F16: return launch_bulk_variant<__half>(a, n_delta, variant, s);
+    default: return BSP_ERR_UNSUPPORTED;
+  }
+}
+
+int launch_proto_sums_bulk(const SpmmArgs& a, int variant, cudaStream_t s) {
+  if (a.n_proto == 0 || a.N == 0) return BSP_OK;
+  switch (a.bdt) {
+    case BSP_F32: return launch_sums_bulk_v<float>(a, variant, s);
+    case BSP_BF16: return launch_sums_bulk_v<__nv_bfloat16>(a, variant, s);
+    case BSP_F16: return launch_sums_bulk_v<__half>(a, variant, s);
     default: return BSP_ERR_UNSUPPORTED;
   }
 }

@@ -69,7 +69,7 @@ bool parse_file(const char* path, std::map<std::string, TuneSched>& out) {
                  "\"tc_tps\": %d, \"tc_tiled\": %d, \"tc_split\": %d, \"ms\": %lf",
                  key, &t.engine, &t.proto_path, &t.proto_variant, &t.tc_tps, &t.tc_tiled, &t.tc_split, &ms) != 8 ||
           (t.engine != 1 && t.engine != 2) || t.proto_path < 0 || t.proto_path > 1 || t.proto_variant < 0 ||
-          t.proto_variant > 7 || (t.tc_tps != 0 && t.tc_tps != 2 && t.tc_tps != 3) || t.tc_tiled < -1 ||
+          t.proto_variant > 8 || (t.tc_tps != 0 && t.tc_tps != 2 && t.tc_tps != 3) || t.tc_tiled < -1 ||
           t.tc_tiled > 1 || t.tc_split < -1 || t.tc_split > 0) {
         ok = false;
         break;

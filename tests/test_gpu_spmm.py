@@ -401,3 +401,39 @@ def test_probe_gather_runs_and_checks_its_arguments():
     assert capi.lib().bsp_probe_gather(ctypes.c_void_p(buf.data_ptr()), rows, 1024,
                                        ctypes.c_void_p(idx.data_ptr()), n_warps, per_warp, 2048,
                                        ctypes.c_void_p(sink.data_ptr()), None) == -2
+
+
+_SUMS_SCRIPT = r"""
+import sys, numpy as np, torch
+sys.path.insert(0, sys.argv[1])
+from bitwise_spgemm_gb300 import capi, ops
+from bitwise_spgemm_gb300 import workloads as W
+A, _, _ = W.clustered_bits(1024, 3000, n_proto=5, p_proto=0.08, p_flip=0.004, seed_proto=5, seed_rows=6)
+words = W.pack_bits(A)
+wd = torch.from_numpy(np.ascontiguousarray(words).view(np.int32)).cuda()
+plan = ops.Plan(wd, 3000, mode=capi.PLAN_PROTO)
+B = np.random.default_rng(7).integers(-8, 9, (3000, 520)).astype(np.float32)
+C = ops.spmm(wd, 3000, torch.from_numpy(B).cuda(), plan=plan)
+torch.cuda.synchronize()
+assert capi.device_status() == 0
+np.save(sys.argv[2], C.cpu().numpy())
+"""
+
+
+@pytest.mark.parametrize("form", ["-1", "0", "1"])
+def test_prototype_sum_forms(tmp_path, form):
+    """Each prototype-sum form (BSP_SUMS_BULK: -1 the cluster form over the
+    column lists, n >= 0 a bulk-copy staging shape; read once per process, so
+    each runs in a child process) gives the exact integer product."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = tmp_path / "C.npy"
+    env = dict(os.environ, BSP_SUMS_BULK=form)
+    r = subprocess.run([sys.executable, "-c", _SUMS_SCRIPT, root, str(out)], env=env, capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    A, _, _ = W.clustered_bits(1024, 3000, n_proto=5, p_proto=0.08, p_flip=0.004, seed_proto=5, seed_rows=6)
+    B = np.random.default_rng(7).integers(-8, 9, (3000, 520)).astype(np.float32)
+    assert np.array_equal(np.load(out).astype(np.float64), O.spmm_f64(W.pack_bits(A), 3000, B))
