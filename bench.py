@@ -406,15 +406,16 @@ def run_ours(args):
     # the remainder as graphs of 4, 2 and 1 steps (buffers 0.., the 8-step
     # rotation having used them long before)
     g1 = [capture(range(k)) for k in (4, 2, 1) if rem & k]
-    for _ in range(max(1, args.warmup // ROTATE)):
+    sampler = ClockSampler(local) if rank == 0 else None
+    if sampler:
+        sampler.start()
+    # warm-up right before the timed region (at least 3 rotations, so that a
+    # short run is not timed while the clocks come up from the set-up)
+    for _ in range(max(3, args.warmup // ROTATE)):
         g.replay()
     for gr in g1:  # a graph's first launch uploads it: keep that out of the timed region
         gr.replay()
     torch.cuda.synchronize()
-
-    sampler = ClockSampler(local) if rank == 0 else None
-    if sampler:
-        sampler.start()
     # per-rotation timing (one graph of 8 steps per event pair), then the total
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * max(reps, 1))]
     barrier(ws)
