@@ -473,12 +473,14 @@ __device__ __forceinline__ int xor_popcount(const uint32_t* __restrict__ a, cons
 // Warp per row: the row's bucket cluster and the clusters sharing one of its
 // pair bands compete on Hamming distance; the row keeps the winner only if
 // the delta is smaller than its popcount.
+constexpr int kOrderBuckets = 256;  // row-slot order: clustered rows counted by min(delta count, 255)
+
 __global__ void __launch_bounds__(256) k_finalize_rows(
     const uint32_t* __restrict__ words, int64_t M, int Kw, int H, const uint32_t* __restrict__ sig,
     const int32_t* __restrict__ nnz, const uint32_t* __restrict__ cons, int64_t n_clusters,
     const uint32_t* __restrict__ akeys, const int32_t* __restrict__ avals, uint32_t amask,
     int32_t* __restrict__ cluster, int32_t* __restrict__ delta_cnt,
-    unsigned long long* __restrict__ stats) {
+    unsigned long long* __restrict__ stats, int32_t* __restrict__ order_hist) {
   const int lane = threadIdx.x & 31;
   const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   if (row >= M) return;
@@ -506,8 +508,10 @@ __global__ void __launch_bounds__(256) k_finalize_rows(
     cluster[row] = c;
     delta_cnt[row] = c >= 0 ? d : 0;
     atomicAdd(stats + 0, (unsigned long long)n);                  // nnz
-    if (c >= 0) atomicAdd(stats + 1, (unsigned long long)d);      // delta entries
-    else {
+    if (c >= 0) {
+      atomicAdd(stats + 1, (unsigned long long)d);                // delta entries
+      atomicAdd(order_hist + (d < kOrderBuckets - 1 ? d : kOrderBuckets - 1), 1);
+    } else {
       atomicAdd(stats + 2, 1ull);                                 // direct rows
       atomicAdd(stats + 3, (unsigned long long)n);                // direct nnz
     }
@@ -518,69 +522,15 @@ __global__ void __launch_bounds__(256) k_finalize_rows(
 // ---- row slots: clustered rows by descending delta count -----------------
 // The SpMM's warps take clustered rows in slot order, and the GPU starts CTAs
 // in index order, so the longest lists start first and the last CTAs to
-// start carry the shortest ones (a shorter tail).  A stable counting sort on
-// min(count, 255): per-block bucket counts, one scan over (bucket
-// descending, block), then each row's rank among the same bucket's earlier
-// rows in its block.
-constexpr int kOrderBuckets = 256;
-__device__ __forceinline__ int order_bucket(const int32_t* cluster, const int32_t* dptr, int64_t row, int64_t M) {
-  if (row >= M || cluster[row] < 0) return -1;
-  const int n = dptr[row + 1] - dptr[row];
-  return n < kOrderBuckets - 1 ? n : kOrderBuckets - 1;
-}
-
-__global__ void __launch_bounds__(256) k_order_count(const int32_t* __restrict__ cluster,
-                                                     const int32_t* __restrict__ dptr, int64_t M, int64_t nb,
-                                                     int32_t* __restrict__ cnt) {
-  __shared__ int h[kOrderBuckets];
-  h[threadIdx.x] = 0;
-  __syncthreads();
-  const int b = order_bucket(cluster, dptr, (int64_t)blockIdx.x * 256 + threadIdx.x, M);
-  if (b >= 0) atomicAdd(&h[b], 1);
-  __syncthreads();
-  cnt[(int64_t)(kOrderBuckets - 1 - threadIdx.x) * nb + blockIdx.x] = h[threadIdx.x];
-}
-
-__global__ void __launch_bounds__(256) k_order_scatter(const int32_t* __restrict__ cluster,
-                                                       const int32_t* __restrict__ dptr, int64_t M, int64_t nb,
-                                                       const int32_t* __restrict__ base, int32_t* __restrict__ order) {
-  __shared__ int wc[8][kOrderBuckets];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int i = threadIdx.x; i < 8 * kOrderBuckets; i += 256) (&wc[0][0])[i] = 0;
-  __syncthreads();
-  const int64_t row = (int64_t)blockIdx.x * 256 + threadIdx.x;
-  const int b = order_bucket(cluster, dptr, row, M);
-  const unsigned peers = __match_any_sync(0xffffffffu, b);
-  const int rank = __popc(peers & ((1u << lane) - 1u));
-  if (b >= 0 && rank == 0) wc[w][b] = __popc(peers);
-  __syncthreads();
-  if (b < 0) return;
-  int before = rank;
-  for (int u = 0; u < w; u++) before += wc[u][b];
-  order[base[(int64_t)(kOrderBuckets - 1 - b) * nb + blockIdx.x] + before] = (int32_t)row;
-}
-
-// Warp per slot p: the 128-byte slot of row order[p] holds the row, its
-// cluster, its delta count, the list's start and the first 28 entries, so
-// the SpMM reads a row's whole description with one load whose address
-// depends on p alone.
-__global__ void __launch_bounds__(256) k_delta_slots(const int32_t* __restrict__ order, int64_t n_slot,
-                                                     const int32_t* __restrict__ cluster,
-                                                     const int32_t* __restrict__ dptr,
-                                                     const uint32_t* __restrict__ didx, uint32_t* __restrict__ pad) {
-  const int lane = threadIdx.x & 31;
-  const int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  if (p >= n_slot) return;
-  const int row = order[p];
-  const int s = dptr[row], n = dptr[row + 1] - s;
-  uint32_t v;
-  if (lane == 0) v = (uint32_t)row;
-  else if (lane == 1) v = (uint32_t)cluster[row];
-  else if (lane == 2) v = (uint32_t)n;
-  else if (lane == 3) v = (uint32_t)s;
-  else v = lane - 4 < n ? didx[s + lane - 4] : 0u;
-  pad[p * 32 + lane] = v;
-}
+// start carry the shortest ones (a shorter tail).  A counting sort on
+// b = min(count, 255): k_finalize_rows counts the rows of each b, and
+// k_delta_fill's blocks each scan those 256 counts (descending b) before
+// every clustered row takes the next position of its b.  Rows with equal b
+// land in any order: the plan's layout depends on it, the SpMM's results do
+// not (each row's sum is formed the same way wherever it sits).  A row's
+// slot holds the row, its cluster, its delta count, the list's start and the
+// first 28 entries, so the SpMM reads a row's whole description with one
+// load whose address depends on the position alone.
 
 // Warp per prototype: its set columns in ascending order into
 // cons_idx[cons_ptr[c] ..] (the list the prototype-sum kernel walks).
@@ -611,20 +561,50 @@ __global__ void __launch_bounds__(256) k_cons_fill(const uint32_t* __restrict__ 
   }
 }
 
-// Warp per clustered row: delta entries in ascending column order.
+// Warp per clustered row: delta entries in ascending column order, and with
+// `pad` the row's slot (position from the bucket counts `hist`, the next
+// free one of its bucket by `cursor`).
 __global__ void __launch_bounds__(256) k_delta_fill(const uint32_t* __restrict__ words, int64_t M,
                                                     int Kw, const uint32_t* __restrict__ cons,
                                                     const int32_t* __restrict__ cluster,
                                                     const int32_t* __restrict__ dptr,
-                                                    uint32_t* __restrict__ didx) {
+                                                    uint32_t* __restrict__ didx, const int32_t* __restrict__ hist,
+                                                    int32_t* __restrict__ cursor, uint32_t* __restrict__ pad) {
+  __shared__ int bucket_base[kOrderBuckets];
+  __shared__ int wsum[8];
   const int lane = threadIdx.x & 31;
+  if (pad) {  // bucket_base[b] = clustered rows with a larger bucket (scan over t = 255 - b)
+    const int h = hist[kOrderBuckets - 1 - threadIdx.x];
+    int v = h;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int u = __shfl_up_sync(kFull, v, o);
+      if (lane >= o) v += u;
+    }
+    if (lane == 31) wsum[threadIdx.x >> 5] = v;
+    __syncthreads();
+    for (int u = 0; u < (int)(threadIdx.x >> 5); u++) v += wsum[u];
+    bucket_base[kOrderBuckets - 1 - threadIdx.x] = v - h;
+    __syncthreads();
+  }
   const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   if (row >= M) return;
   const int c = cluster[row];
   if (c < 0) return;
   const uint32_t* r = words + row * Kw;
   const uint32_t* p = cons + (int64_t)c * Kw;
-  int base = dptr[row];
+  const int s0 = dptr[row];
+  uint32_t* slot = nullptr;
+  if (pad) {
+    const int n = dptr[row + 1] - s0;
+    const int b = n < kOrderBuckets - 1 ? n : kOrderBuckets - 1;
+    int at = 0;
+    if (lane == 0) at = bucket_base[b] + atomicAdd(&cursor[b], 1);
+    slot = pad + (int64_t)__shfl_sync(kFull, at, 0) * 32;
+    if (lane < 4) slot[lane] = lane == 0 ? (uint32_t)row : lane == 1 ? (uint32_t)c : lane == 2 ? (uint32_t)n : (uint32_t)s0;
+    else if (lane - 4 >= n) slot[lane] = 0u;
+  }
+  int base = s0;
   for (int w0 = 0; w0 < Kw; w0 += 32) {
     const int w = w0 + lane;
     const uint32_t a = w < Kw ? r[w] : 0u;
@@ -641,7 +621,10 @@ __global__ void __launch_bounds__(256) k_delta_fill(const uint32_t* __restrict__
     while (x) {
       const int b = __ffs(x) - 1;
       x &= x - 1;
-      didx[pos++] = (uint32_t)(w * 32 + b) | (((q >> b) & 1u) ? 0x80000000u : 0u);
+      const uint32_t e = (uint32_t)(w * 32 + b) | (((q >> b) & 1u) ? 0x80000000u : 0u);
+      didx[pos] = e;
+      if (slot && pos - s0 < 28) slot[4 + pos - s0] = e;
+      pos++;
     }
     base += __shfl_sync(kFull, incl, 31);
   }
@@ -899,8 +882,9 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
   const size_t o_flag = take(sizeof(int32_t) * M);
   const size_t o_cid = take(sizeof(int32_t) * (M + 1));
   const size_t o_coff = take(sizeof(int32_t) * (M + 1));
-  const size_t o_scan = take(scan_workspace_bytes(M + kOrderBuckets + 1));
-  const size_t o_stats = take(sizeof(unsigned long long) * 8);
+  const size_t o_scan = take(scan_workspace_bytes(M + 1));
+  // stats[8], then the row-slot order's bucket counts and cursors
+  const size_t o_stats = take(sizeof(unsigned long long) * 8 + sizeof(int32_t) * 2 * kOrderBuckets);
   const size_t o_dcnt = take(sizeof(int32_t) * M);
   DevBuf tmp;
   BSP_TRY(tmp.alloc(off, s));
@@ -916,10 +900,11 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
   int32_t* coff = (int32_t*)(T + o_coff);
   void* scanws = T + o_scan;
   unsigned long long* stats = (unsigned long long*)(T + o_stats);
+  int32_t* order_hist = (int32_t*)(stats + 8);
   int32_t* dcnt = (int32_t*)(T + o_dcnt);
 
   BSP_TRY(launch_fill4(Fill{keys, tsize, kEmpty}, Fill{(uint32_t*)cnt, tsize, 0u},
-                       Fill{(uint32_t*)lead, tsize, 0x7f7f7f7fu}, Fill{(uint32_t*)stats, 16, 0u}, s));
+                       Fill{(uint32_t*)lead, tsize, 0x7f7f7f7fu}, Fill{(uint32_t*)stats, 16 + 2 * kOrderBuckets, 0u}, s));
 
   // ---- tensor-core structures: occupancy bitmaps and A's words by column
   // (the producers then load the words of 32 consecutive rows or columns as
@@ -1013,13 +998,13 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
     BSP_LAUNCHED();
     BSP_TRY(launch_scan_i32(ccnt, ncl, plan->cons_ptr, scanws, s));
     k_finalize_rows<<<wgrid, 256, 0, s>>>(words, M, Kw, H, sig, nnz, plan->cons, ncl, akeys, avals,
-                                          asize - 1, plan->row_cluster, dcnt, stats);
+                                          asize - 1, plan->row_cluster, dcnt, stats, order_hist);
     BSP_LAUNCHED();
   } else {
     BSP_CUDA(cudaMemsetAsync(plan->row_cluster, 0xff, sizeof(int32_t) * M, s));
     BSP_CUDA(cudaMemsetAsync(dcnt, 0, sizeof(int32_t) * M, s));
     k_finalize_rows<<<wgrid, 256, 0, s>>>(words, M, Kw, H, sig, nnz, plan->cons, 0, nullptr,
-                                          nullptr, 0, plan->row_cluster, dcnt, stats);
+                                          nullptr, 0, plan->row_cluster, dcnt, stats, order_hist);
     BSP_LAUNCHED();
   }
   BSP_TRY(launch_scan_i32(dcnt, M, plan->delta_ptr, scanws, s));
@@ -1064,25 +1049,11 @@ int plan_build(const uint32_t* words, int64_t M, int64_t K, const bsp_plan_param
     plan->delta_pad = n_pad > 0 ? (uint32_t*)plan->delta_arena : nullptr;
     plan->delta_idx = (uint32_t*)plan->delta_arena + n_pad;
     plan->cons_idx = n_list > 0 ? plan->delta_idx + plan->delta_nnz : nullptr;
-    if (plan->delta_nnz > 0)
-      k_delta_fill<<<wgrid, 256, 0, s>>>(words, M, Kw, plan->cons, plan->row_cluster,
-                                         plan->delta_ptr, plan->delta_idx);
-    if (n_pad > 0) {
-      const int64_t nb = ceil_div(M, 256), nc = kOrderBuckets * nb;
-      DevBuf ob;
-      BSP_TRY(ob.alloc(sizeof(int32_t) * (size_t)(n_slot + 2 * nc + 1), s));
-      int32_t* order = static_cast<int32_t*>(ob.p);
-      int32_t* cnt = order + n_slot;
-      int32_t* base = cnt + nc;
-      k_order_count<<<(unsigned)nb, 256, 0, s>>>(plan->row_cluster, plan->delta_ptr, M, nb, cnt);
-      BSP_LAUNCHED();
-      BSP_TRY(launch_scan_i32(cnt, nc, base, scanws, s));
-      k_order_scatter<<<(unsigned)nb, 256, 0, s>>>(plan->row_cluster, plan->delta_ptr, M, nb, base, order);
-      k_delta_slots<<<(unsigned)ceil_div(n_slot, 8), 256, 0, s>>>(order, n_slot, plan->row_cluster,
-                                                                   plan->delta_ptr, plan->delta_idx, plan->delta_pad);
-      BSP_LAUNCHED();
-      plan->n_slot = n_slot;
-    }
+    if (plan->delta_nnz > 0 || n_pad > 0)
+      k_delta_fill<<<wgrid, 256, 0, s>>>(words, M, Kw, plan->cons, plan->row_cluster, plan->delta_ptr,
+                                         plan->delta_idx, order_hist, order_hist + kOrderBuckets,
+                                         plan->delta_pad);
+    plan->n_slot = n_pad > 0 ? n_slot : 0;
     if (n_list > 0)
       k_cons_fill<<<(unsigned)ceil_div(ncl, 8), 256, 0, s>>>(plan->cons, ncl, Kw, plan->cons_ptr, plan->cons_idx);
     BSP_LAUNCHED();
