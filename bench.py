@@ -642,6 +642,8 @@ def run_batched(args, emit=True):
         comp += M * ((K + 31) // 32) * 4 + K * N * 2 + M * N * 4
         nnz += int(np.unpackbits(np.ascontiguousarray(pr["words"]).view(np.uint8)).sum())
     batch = ops.Batch(items)
+    # the batch's own tuner picks the persistent kernel's shape (before capture)
+    shape, tune_ms = batch.tune()
 
     def graph_of(fn):
         fn()
@@ -697,7 +699,9 @@ def run_batched(args, emit=True):
            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "bf16", "data": "synthetic (seeded numpy, seed 7+i per problem)",
            "config": {"workload": "batched_512_N128_bf16", "problems": len(probs), "N": N,
-                      "nnz": nnz, "graph": "one persistent launch (a CTA per SM taking 256-row items from a device work queue), graph-captured"},
+                      "nnz": nnz, "graph": "one persistent launch (a CTA per SM taking 256-row items from a device work queue), graph-captured",
+                      "kernel_shape": {"index": shape, "tuned_ms": tune_ms,
+                                       "by": "bsp_batch_tune (stages, epilogue warps, A words ahead)"}},
            "aggregate_gbs": ws * comp / (ms * 1e-3) / 1e9,
            "effective_tflops": 2.0 * nnz * N / (ms * 1e-3) / 1e12,
            "fp32_loop_ms": ms32, "speedup_vs_fp32_loop": ms32 / ms,

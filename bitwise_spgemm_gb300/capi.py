@@ -84,6 +84,7 @@ SIGNATURES = {
     "bsp_batch_create": [C.POINTER(Problem), _I, _I64, _I, C.POINTER(_P), _P],
     "bsp_batch_destroy": [_P],
     "bsp_batched_spmm": [_P, _P],
+    "bsp_batch_tune": [_P, _P, C.POINTER(_I), C.POINTER(C.c_float)],
     "bsp_batch_grad_create": [C.POINTER(ProblemGrad), _I, _I64, _I, C.POINTER(_P), _P],
     "bsp_batched_spmm_grad": [_P, _P],
     "bsp_probe_gather": [_P, _I64, _I64, _P, _I64, _I64, _I, _P, _P],

@@ -63,7 +63,7 @@ constexpr int64_t kItemRows = 256, kItemCols = 256;  // the tensor-core kernel's
 // from a counter.  Every wait is bounded: on timeout the role records error
 // 4 in g_batch_error and stops; the others' bounded waits then end.
 constexpr int kPRows = 256, kPM = 128, kPK = 32, kPMaxN = 128;
-constexpr int kPTps = 2, kPStages = 3, kPQ = 4;
+constexpr int kPTps = 2, kPQ = 4;
 constexpr int kPATile = kPRows * kPK * 2;  // 16 KB: both halves of one K tile
 constexpr int kPAHalf = kPM * kPK * 2;     // 8 KB
 constexpr int kPBox = 64 * kPK * 2;        // 4 KB: 64 columns x 32 rows
@@ -71,25 +71,24 @@ constexpr int kPBTile = 2 * kPBox;         // 8 KB: up to 128 columns
 constexpr int kPAStage = kPTps * kPATile, kPBStage = kPTps * kPBTile;
 constexpr int kPProdWarps = kPRows / 32;  // 8
 constexpr int kPTmaWarp = kPProdWarps, kPMmaWarp = kPProdWarps + 1;
-constexpr int kPEpiWarp0 = kPProdWarps + 2, kPEpiWarps = 8;
-constexpr int kPThreads = (kPEpiWarp0 + kPEpiWarps) * 32;  // 576
+constexpr int kPEpiWarp0 = kPProdWarps + 2;
 constexpr int kPEpiStride = 36;       // staging rows 36 floats apart (16-byte aligned, conflict-free)
 constexpr uint32_t kPTmemCols = 512;  // two sets x two halves x 128 columns
-constexpr int kPWordAhead = 4;
 constexpr int kPErr = 4;
 
+// STAGES pipeline stages (32 KB of A + 16 KB of B each), EPIW epilogue warps
+template <int STAGES, int EPIW>
 struct __align__(1024) PersistSmem {
-  uint8_t a[kPStages * kPAStage];  // 96 KB
-  uint8_t b[kPStages * kPBStage];  // 48 KB, 1 KB-aligned (128-byte swizzle atoms)
-  float epi[kPEpiWarps][32 * kPEpiStride];
-  uint64_t full[kPStages], empty[kPStages];
+  uint8_t a[STAGES * kPAStage];
+  uint8_t b[STAGES * kPBStage];  // 1 KB-aligned (128-byte swizzle atoms)
+  float epi[EPIW][32 * kPEpiStride];
+  uint64_t full[STAGES], empty[STAGES];
   uint64_t tfull[2], tempty[2];
   uint64_t qfull[kPQ], qempty[kPQ];
   int qitem[kPQ];
   uint32_t tmem_addr;
 };
 constexpr size_t kPSmemAlign = 1024;
-static_assert(sizeof(PersistSmem) + kPSmemAlign <= 232448, "persistent batched kernel: shared memory");
 
 __device__ __forceinline__ void persist_fail() { atomicCAS(&g_batch_error, 0, kPErr); }
 
@@ -105,12 +104,16 @@ __device__ __forceinline__ bool warp_wait_read(uint64_t* bar, uint32_t parity, c
   return ok != 0;
 }
 
-template <typename BT>
-__global__ void __launch_bounds__(kPThreads, 1)
+template <typename BT, int STAGES, int EPIW, int WA>
+__global__ void __launch_bounds__((kPEpiWarp0 + EPIW) * 32, 1)
     k_batched_persist(const BatchProblemTc* __restrict__ probs, const int4* __restrict__ items, int n_items,
                       int* next_item, int64_t N) {
+  constexpr int kPStages = STAGES, kPEpiWarps = EPIW, kPWordAhead = WA;
+  using Smem = PersistSmem<STAGES, EPIW>;
+  static_assert(sizeof(Smem) + kPSmemAlign <= 232448, "persistent batched kernel: shared memory");
+  static_assert(EPIW == 4 || EPIW == 8, "epilogue warps cover the four TMEM lane quarters");
   extern __shared__ __align__(1024) uint8_t smem_raw[];
-  PersistSmem& sm = *reinterpret_cast<PersistSmem*>(
+  Smem& sm = *reinterpret_cast<Smem*>(
       smem_raw + ((kPSmemAlign - (ptx::smem_addr(smem_raw) & (kPSmemAlign - 1))) & (kPSmemAlign - 1)));
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nbox = (int)((min(N, (int64_t)kPMaxN) + 63) / 64);  // 64-column boxes holding output columns
@@ -294,9 +297,10 @@ __global__ void __launch_bounds__(kPThreads, 1)
     }
   } else {
     // ---------------- epilogue ----------------
-    const int e = warp - kPEpiWarp0;  // 0..7
+    const int e = warp - kPEpiWarp0;  // 0..EPIW-1
     const int q4 = warp & 3;          // the TMEM lane quarter this warp may access
-    const int ch = e >> 2;            // column half
+    // column halves of this warp: one of the two with 8 epilogue warps, both with 4
+    const int ch0 = EPIW == 8 ? e >> 2 : 0, ch1 = EPIW == 8 ? (e >> 2) + 1 : 2;
     const int cspan = nbox * 32;      // live columns per half (a multiple of 32)
     float* tile = sm.epi[e];
     for (int j = 0;; j++) {
@@ -317,7 +321,8 @@ __global__ void __launch_bounds__(kPThreads, 1)
         break;
       }
       ptx::tc_fence_after_sync();
-      for (int h = 0; h < 2; h++) {
+      for (int hc = 0; hc < 2 * (ch1 - ch0); hc++) {
+        const int h = hc & 1, ch = ch0 + (hc >> 1);
         const int64_t rbase = (int64_t)w4.y * kPRows + h * kPM + q4 * 32;  // the warp's first row
         if (rbase >= M) continue;
         const uint32_t tb = tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(set * 256 + h * kPM + ch * cspan);
@@ -371,22 +376,39 @@ __global__ void __launch_bounds__(kPThreads, 1)
   }
 }
 
-template <typename BT>
-int launch_persist_t(const BatchProblemTc* probs, const int4* items, int n_items, int* counter, int64_t N,
+template <typename BT, int STAGES, int EPIW, int WA>
+int launch_persist_s(const BatchProblemTc* probs, const int4* items, int n_items, int* counter, int64_t N,
                      cudaStream_t st) {
-  constexpr size_t smem = sizeof(PersistSmem) + kPSmemAlign;
+  constexpr size_t smem = sizeof(PersistSmem<STAGES, EPIW>) + kPSmemAlign;
+  auto kern = k_batched_persist<BT, STAGES, EPIW, WA>;
   static bool configured[64] = {false};
   int dev = 0;
   BSP_CUDA(cudaGetDevice(&dev));
   if (dev >= 64 || !configured[dev]) {
-    BSP_CUDA(cudaFuncSetAttribute(k_batched_persist<BT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    BSP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     if (dev < 64) configured[dev] = true;
   }
   BSP_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), st));
   const int grid = std::min(num_sms(), n_items);
-  k_batched_persist<BT><<<grid, kPThreads, smem, st>>>(probs, items, n_items, counter, N);
+  kern<<<grid, (kPEpiWarp0 + EPIW) * 32, smem, st>>>(probs, items, n_items, counter, N);
   BSP_LAUNCHED();
   return BSP_OK;
+}
+
+// Shapes of the persistent kernel (pipeline stages, epilogue warps, A words
+// loaded ahead), chosen per batch by bsp_batch_tune.  At the 512-problem N =
+// 128 set: 3/4/4 192.6 us, 3/8/4 196.8 (its 576 threads spill 44 bytes at
+// 96 registers), 3/8/8 198.9, 4/4/4 202.3, 4/4/8 206.8.
+constexpr int kPersistShapes = 4;
+template <typename BT>
+int launch_persist_t(const BatchProblemTc* probs, const int4* items, int n_items, int* counter, int64_t N,
+                     int shape, cudaStream_t st) {
+  switch (shape) {
+    case 1: return launch_persist_s<BT, 3, 8, 4>(probs, items, n_items, counter, N, st);
+    case 2: return launch_persist_s<BT, 4, 4, 4>(probs, items, n_items, counter, N, st);
+    case 3: return launch_persist_s<BT, 3, 4, 8>(probs, items, n_items, counter, N, st);
+    default: return launch_persist_s<BT, 3, 4, 4>(probs, items, n_items, counter, N, st);
+  }
 }
 
 }  // namespace
@@ -408,6 +430,7 @@ struct bsp_batch {
   int4* items = nullptr;
   int4* items_s = nullptr;
   int* counter = nullptr;  // next item of the persistent kernel (reset by every run)
+  int shape = 0;           // persistent kernel's shape (bsp_batch_tune)
 };
 
 namespace {
@@ -609,11 +632,59 @@ int bsp_batched_spmm(const bsp_batch* b, bsp_stream_t stream) {
   // launch, for comparisons); wider N: a CTA per (256-row, 256-column) item
   const char* e = getenv("BSP_BATCH_PERSIST");
   if (b->N <= kPMaxN && !(e && e[0] == '0')) {
-    if (b->bdt == BSP_BF16) return launch_persist_t<__nv_bfloat16>(b->probs, b->items, b->n_items, b->counter, b->N, s);
-    if (b->bdt == BSP_F16) return launch_persist_t<__half>(b->probs, b->items, b->n_items, b->counter, b->N, s);
+    if (b->bdt == BSP_BF16)
+      return launch_persist_t<__nv_bfloat16>(b->probs, b->items, b->n_items, b->counter, b->N, b->shape, s);
+    if (b->bdt == BSP_F16)
+      return launch_persist_t<__half>(b->probs, b->items, b->n_items, b->counter, b->N, b->shape, s);
     return BSP_ERR_UNSUPPORTED;
   }
   return launch_batched_tc(b->probs, b->items, b->n_items, b->N, b->bdt, s);
+}
+
+int bsp_batch_tune(bsp_batch* b, bsp_stream_t stream, int* shape, float* ms) {
+  using namespace bsp;
+  if (!b || b->grad || !shape || !ms) return BSP_ERR_INVALID_ARG;
+  int dev = -1;
+  cudaGetDevice(&dev);
+  if (dev != b->device) return BSP_ERR_INVALID_ARG;
+  const cudaStream_t s = (cudaStream_t)stream;
+  const char* e = getenv("BSP_BATCH_PERSIST");
+  const int n_shapes = (b->N <= kPMaxN && !(e && e[0] == '0')) ? kPersistShapes : 1;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int best = 0;
+  float best_ms = 0.f;
+  const int keep = b->shape;
+  auto sweep = [&]() -> int {
+    BSP_CUDA(cudaEventCreate(&e0));
+    BSP_CUDA(cudaEventCreate(&e1));
+    for (int v = 0; v < n_shapes; v++) {
+      b->shape = v;
+      BSP_TRY(bsp_batched_spmm(b, stream));  // warm-up (first launch of this shape)
+      BSP_CUDA(cudaEventRecord(e0, s));
+      for (int r = 0; r < 3; r++) BSP_TRY(bsp_batched_spmm(b, stream));
+      BSP_CUDA(cudaEventRecord(e1, s));
+      BSP_CUDA(cudaEventSynchronize(e1));
+      float t = 0.f;
+      BSP_CUDA(cudaEventElapsedTime(&t, e0, e1));
+      t /= 3.f;
+      if (v == 0 || t < best_ms) {
+        best = v;
+        best_ms = t;
+      }
+    }
+    return BSP_OK;
+  };
+  const int rc = sweep();
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (rc != BSP_OK) {
+    b->shape = keep;
+    return rc;
+  }
+  b->shape = best;
+  *shape = best;
+  *ms = best_ms;
+  return BSP_OK;
 }
 
 int bsp_batched_spmm_grad(const bsp_batch* b, bsp_stream_t stream) {

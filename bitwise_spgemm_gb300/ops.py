@@ -433,6 +433,13 @@ class Batch:
     def run(self):
         call("bsp_batched_spmm", self._h, _stream())
 
+    def tune(self):
+        """Time the persistent kernel's shapes on this batch (runs it 16
+        times), keep the fastest for later runs; returns (shape, ms)."""
+        shape, ms = C.c_int(), C.c_float()
+        call("bsp_batch_tune", self._h, _stream(), C.byref(shape), C.byref(ms))
+        return shape.value, ms.value
+
     def close(self):
         if getattr(self, "_h", None):
             self._lib.bsp_batch_destroy(self._h)

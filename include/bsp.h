@@ -268,6 +268,13 @@ int bsp_batch_destroy(bsp_batch* batch);
  * resets first.  For wider N it is one CTA per work item.  Runs of one batch
  * must not overlap on the GPU: they share the queue and the C buffers.     */
 int bsp_batched_spmm(const bsp_batch* batch, bsp_stream_t stream);
+/* Times the persistent kernel's shapes (pipeline stages, epilogue warps, A
+ * words loaded ahead) on this batch — each once to warm up, then three runs
+ * — keeps the fastest in the batch for later bsp_batched_spmm calls and
+ * returns its index and ms per run.  It runs the batch (writes its C
+ * buffers) 16 times and synchronises the stream.  Batches of N > 128 have
+ * one shape (index 0).  On an error the batch keeps its previous shape. */
+int bsp_batch_tune(bsp_batch* batch, bsp_stream_t stream, int* shape, float* ms);
 
 /* One problem of a batched backward pass of Y = A·X (A a 0/1 mask, packed
  * LSB-first words [M][ceil(K/32)]; X [K×N] and the incoming gradient

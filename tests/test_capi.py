@@ -74,6 +74,9 @@ def test_argument_validation_without_gpu():
     assert L.bsp_batch_grad_create(None, 0, 8, 0, C.byref(h), None) == -4
     assert L.bsp_batch_grad_create(None, 0, 12, 2, C.byref(h), None) == -2
     assert L.bsp_batched_spmm_grad(None, None) == -1
+    # batch tuner: null batch or out-pointers
+    shape, ms = C.c_int(), C.c_float()
+    assert L.bsp_batch_tune(None, None, C.byref(shape), C.byref(ms)) == -1
     # L2 gather probe: slice size, alignment, warp count
     assert L.bsp_probe_gather(fake, 8, 2048, fake, 8, 4, 384, fake, None) == -1
     assert L.bsp_probe_gather(P(0x10004), 8, 2048, fake, 8, 4, 512, fake, None) == -2

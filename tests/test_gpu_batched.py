@@ -236,3 +236,26 @@ def test_batched_set_real_shapes_against_fp64():
         sc = (np.abs(G.astype(np.float64)) @ np.abs(X.astype(np.float64)).T)[A]
         assert np.all(dA[~A] == 0.0)
         assert (np.abs(dA[A] - v64) / np.where(sc > 0, sc, 1.0)).max() <= TOL, (i, "dA")
+
+
+def test_batch_tune_keeps_results_exact():
+    """bsp_batch_tune times every shape of the persistent kernel, keeps the
+    fastest, and each shape gives the same exact integer products."""
+    N = 128
+    probs = _problems(20, N, seed=31, integer=True)
+    dev = _run(probs, N)
+    batch = ops.Batch(dev)
+    shape, ms = batch.tune()
+    assert 0 <= shape < 4 and ms > 0
+    for _, _, _, Cd in dev:
+        Cd.fill_(float("nan"))
+    batch.run()
+    torch.cuda.synchronize()
+    assert capi.device_status() == 0
+    for (words, K, b16), (_, _, _, Cd) in zip(probs, dev):
+        assert np.array_equal(Cd.cpu().numpy().astype(np.float64), O.spmm_f64(words, K, W.bf16_bits_to_f32(b16)))
+    # a batch of N > 128 has one form
+    probs = _problems(4, 200, seed=32, integer=True)
+    dev = _run(probs, 200)
+    batch = ops.Batch(dev)
+    assert batch.tune()[0] == 0
