@@ -12,6 +12,7 @@ namespace bsp {
 struct BatchProblemTc {
   CUtensorMap map;   // forward: B [K][N]; Aᵀ·G: G [M][N] (64x32 boxes); SDDMM: G [M][N] (64x256 boxes)
   CUtensorMap map2;  // SDDMM: X [K][N] (64x256 boxes); otherwise unused
+  CUtensorMap map3;  // SDDMM: G [M][N] in 64x128 boxes (the persistent batched SDDMM); otherwise unused
   const uint32_t* A;
   int64_t M, K, Kw;
   float* C;          // forward: C [M][N]; Aᵀ·G: dX [K][N]; SDDMM: dA [M][K]
@@ -22,7 +23,8 @@ struct BatchProblemTc {
 int make_batch_map(CUtensorMap* m, const void* B, int bdt, int64_t K, int64_t N, int64_t ldb);
 // Tensor map of G [M][N] or X [K][N] for the batched SDDMM: 64-column x
 // 256-row boxes.
-int make_batch_map_sddmm(CUtensorMap* m, const void* T, int bdt, int64_t rows, int64_t N, int64_t ld);
+int make_batch_map_sddmm(CUtensorMap* m, const void* T, int bdt, int64_t rows, int64_t N, int64_t ld,
+                         int box_rows = 256);
 // Work item b = {problem, 256-row block, 256-column block, reduction tiles}:
 // one CTA each.  kind 0 = forward C = A·B, 1 = dX = Aᵀ·G (rows: K),
 // 2 = dA = (G·Xᵀ) ⊙ A (columns: K).

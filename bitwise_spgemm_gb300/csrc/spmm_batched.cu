@@ -411,6 +411,243 @@ int launch_persist_t(const BatchProblemTc* probs, const int4* items, int n_items
   }
 }
 
+// ---- persistent batched SDDMM (dA = (G·Xᵀ) ⊙ A of a gradient batch) -----
+// One CTA per SM takes items — (problem, 128 rows of dA, 256 columns of dA)
+// — from the batch's work queue.  Both operands are dense 16-bit tiles, so
+// there are no producers: the TMA warp loads, per 64 columns of N, G's box
+// (128 rows, 16 KB) and X's box (256 rows, 32 KB), K-major with the 128-byte
+// swizzle; the MMA warp issues four M128 N256 K16 MMAs per stage into
+// accumulator set j % 2 of item j; 8 epilogue warps (two per TMEM lane
+// quarter, one per 128-column half) keep the set bits of A's rows, pass 32
+// columns at a time through a staging tile and store dA rows whole.  With
+// two accumulator sets an item's epilogue — the store of 128 KB of dA, the
+// bound of this write-heavy product — runs under the next item's loads and
+// MMAs instead of after them.  Every wait is bounded (error 4 in
+// g_batch_error).
+constexpr int kSdRows = 128, kSdCols = 256, kSdStep = 64, kSdStages = 3;
+constexpr int kSdGBox = kSdRows * kSdStep * 2;  // 16 KB
+constexpr int kSdXBox = kSdCols * kSdStep * 2;  // 32 KB
+constexpr int kSdEpiWarps = 8, kSdEpiWarp0 = 2;
+constexpr int kSdThreads = (kSdEpiWarp0 + kSdEpiWarps) * 32;  // 320
+
+struct __align__(1024) SddmmSmem {
+  uint8_t g[kSdStages * kSdGBox];  // 1 KB-aligned boxes (128-byte swizzle atoms)
+  uint8_t x[kSdStages * kSdXBox];
+  float epi[kSdEpiWarps][32 * kPEpiStride];
+  uint64_t full[kSdStages], empty[kSdStages];
+  uint64_t tfull[2], tempty[2];
+  uint64_t qfull[kPQ], qempty[kPQ];
+  int qitem[kPQ];
+  uint32_t tmem_addr;
+};
+static_assert(sizeof(SddmmSmem) + kPSmemAlign <= 232448, "persistent SDDMM: shared memory");
+
+template <typename BT>
+__global__ void __launch_bounds__(kSdThreads, 1)
+    k_batched_sddmm_persist(const BatchProblemTc* __restrict__ probs, const int4* __restrict__ items, int n_items,
+                            int* next_item, int64_t N) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  SddmmSmem& sm = *reinterpret_cast<SddmmSmem*>(
+      smem_raw + ((kPSmemAlign - (ptx::smem_addr(smem_raw) & (kPSmemAlign - 1))) & (kPSmemAlign - 1)));
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nst = (int)((N + kSdStep - 1) / kSdStep);  // stages of an item (every item reduces all of N)
+  if (tid == 0) {
+    for (int s = 0; s < kSdStages; s++) {
+      ptx::mbar_init(&sm.full[s], 1);   // the TMA transaction arrival
+      ptx::mbar_init(&sm.empty[s], 1);  // tcgen05.commit of the stage's MMAs
+    }
+    for (int b = 0; b < 2; b++) {
+      ptx::mbar_init(&sm.tfull[b], 1);
+      ptx::mbar_init(&sm.tempty[b], kSdEpiWarps);
+    }
+    for (int q = 0; q < kPQ; q++) {
+      ptx::mbar_init(&sm.qfull[q], 1);
+      ptx::mbar_init(&sm.qempty[q], kSdEpiWarps);
+    }
+    ptx::fence_mbar_init();
+  }
+  if (warp == 1) {
+    ptx::tmem_alloc(&sm.tmem_addr, kPTmemCols);
+    ptx::tmem_relinquish();
+  }
+  ptx::tc_fence_before_sync();
+  __syncthreads();
+  ptx::tc_fence_after_sync();
+  const uint32_t tmem = sm.tmem_addr;
+
+  if (warp == 0) {
+    // ---------------- item queue + G and X by TMA ----------------
+    if (lane == 0) {
+      const uint32_t g0 = ptx::smem_addr(sm.g), x0 = ptx::smem_addr(sm.x), f0 = ptx::smem_addr(&sm.full[0]);
+      uint32_t g = 0;
+      for (int j = 0;; j++) {
+        const int q = j % kPQ;
+        if (j >= kPQ && !ptx::mbar_wait(&sm.qempty[q], (uint32_t)((j / kPQ) - 1) & 1u)) {
+          persist_fail();
+          break;
+        }
+        const int it = atomicAdd(next_item, 1);
+        sm.qitem[q] = it < n_items ? it : -1;
+        ptx::mbar_arrive(&sm.qfull[q]);
+        if (it >= n_items) break;
+        const int4 w4 = __ldg(items + it);
+        const BatchProblemTc* p = probs + w4.x;
+        ptx::tensormap_acquire(&p->map3);  // written by the host into global memory
+        ptx::tensormap_acquire(&p->map2);
+        bool fail = false;
+        for (int i = 0; i < nst; i++, g++) {
+          const int s = (int)(g % kSdStages);
+          if (g >= (uint32_t)kSdStages && !ptx::mbar_wait(&sm.empty[s], ((g / kSdStages) - 1) & 1u)) {
+            persist_fail();
+            fail = true;
+            break;
+          }
+          ptx::mbar_arrive_expect_tx(&sm.full[s], (uint32_t)(kSdGBox + kSdXBox));
+          ptx::tma_load_2d_u32(g0 + (uint32_t)(s * kSdGBox), &p->map3, i * kSdStep, w4.y * kSdRows, f0 + (uint32_t)s * 8u);
+          ptx::tma_load_2d_u32(x0 + (uint32_t)(s * kSdXBox), &p->map2, i * kSdStep, w4.z * kSdCols, f0 + (uint32_t)s * 8u);
+        }
+        if (fail) break;
+      }
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      const uint32_t ab = std::is_same<BT, __nv_bfloat16>::value ? 1u : 0u;
+      const uint32_t idesc = tc::idesc_f16(ab, 0u, 0u, (uint32_t)kSdCols, (uint32_t)kSdRows);
+      const uint64_t gdesc = ptx::smem_desc_noswizzle_u32(ptx::smem_addr(sm.g), 16, 1024) |
+                             ((uint64_t)tc::kLayoutSw128 << 61);
+      const uint64_t xdesc = ptx::smem_desc_noswizzle_u32(ptx::smem_addr(sm.x), 16, 1024) |
+                             ((uint64_t)tc::kLayoutSw128 << 61);
+      uint32_t g = 0;
+      for (int j = 0;; j++) {
+        if (!ptx::mbar_wait(&sm.qfull[j % kPQ], (uint32_t)(j / kPQ) & 1u)) {
+          persist_fail();
+          break;
+        }
+        if (*(volatile const int*)&sm.qitem[j % kPQ] < 0) break;
+        const int set = j & 1;
+        if (j >= 2 && !ptx::mbar_wait(&sm.tempty[set], (uint32_t)((j >> 1) - 1) & 1u)) {
+          persist_fail();
+          break;
+        }
+        ptx::tc_fence_after_sync();
+        const uint32_t dset = tmem + (uint32_t)(set * kSdCols);
+        bool fail = false;
+        for (int i = 0; i < nst; i++, g++) {
+          const int s = (int)(g % kSdStages);
+          if (!ptx::mbar_wait(&sm.full[s], (g / kSdStages) & 1u)) {
+            persist_fail();
+            fail = true;
+            break;
+          }
+          ptx::tc_fence_after_sync();
+#pragma unroll
+          for (int k = 0; k < kSdStep / 16; k++)  // K step k starts 32 B into the 128-byte rows
+            ptx::tc_mma_f16(dset, gdesc + (uint64_t)((s * kSdGBox + k * 32) >> 4),
+                            xdesc + (uint64_t)((s * kSdXBox + k * 32) >> 4), idesc, i > 0 || k > 0);
+          ptx::tc_commit(&sm.empty[s]);
+        }
+        if (fail) break;
+        if (nst > 0) ptx::tc_commit(&sm.tfull[set]);
+        else ptx::mbar_arrive(&sm.tfull[set]);
+      }
+    }
+  } else {
+    // ---------------- epilogue ----------------
+    const int e = warp - kSdEpiWarp0;  // 0..7
+    const int q4 = warp & 3;           // the TMEM lane quarter this warp may access
+    const int ch = e >> 2;             // 128-column half of the item
+    float* tile = sm.epi[e];
+    for (int j = 0;; j++) {
+      int it = -1;
+      if (!warp_wait_read(&sm.qfull[j % kPQ], (uint32_t)(j / kPQ) & 1u, &sm.qitem[j % kPQ], &it)) {
+        if (lane == 0) persist_fail();
+        break;
+      }
+      if (it < 0) break;
+      const int4 w4 = __ldg(items + it);
+      const BatchProblemTc* p = probs + w4.x;
+      const int64_t M = p->M, K = p->K, Kw = p->Kw, ldc = p->ldc;
+      float* C = p->C;
+      const int64_t rbase = (int64_t)w4.y * kSdRows + q4 * 32;  // the warp's first row
+      const int64_t cbase = (int64_t)w4.z * kSdCols + ch * 128;  // its first column
+      // the row's A words of these 128 columns
+      uint32_t aw[4] = {0u, 0u, 0u, 0u};
+      if (rbase + lane < M) {
+        const uint32_t* arow = p->A + (rbase + lane) * Kw;
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+          if (cbase / 32 + i < Kw) aw[i] = __ldg(arow + cbase / 32 + i);
+      }
+      const int set = j & 1;
+      if (!warp_wait_read(&sm.tfull[set], (uint32_t)(j >> 1) & 1u, nullptr, nullptr)) {
+        if (lane == 0) persist_fail();
+        break;
+      }
+      ptx::tc_fence_after_sync();
+      const uint32_t tb = tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(set * kSdCols + ch * 128);
+      for (int c32 = 0; c32 < 4; c32++) {
+        uint32_t v[4][8];
+#pragma unroll
+        for (int u = 0; u < 4; u++) ptx::tmem_ld_32x32b_x8(tb + (uint32_t)(c32 * 32 + u * 8), v[u]);
+        ptx::tmem_wait_ld();
+        const uint32_t wbits = aw[c32];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          float4* t4 = reinterpret_cast<float4*>(tile + lane * kPEpiStride + u * 8);
+          float f[8];
+#pragma unroll
+          for (int x = 0; x < 8; x++) f[x] = ((wbits >> (u * 8 + x)) & 1u) ? __uint_as_float(v[u][x]) : 0.f;
+          t4[0] = make_float4(f[0], f[1], f[2], f[3]);
+          t4[1] = make_float4(f[4], f[5], f[6], f[7]);
+        }
+        __syncwarp();
+        // 8 lanes per row: rows 4*k + lane/8, 16 bytes each
+        const int c4 = (lane & 7) * 4;
+        const int64_t gcol = cbase + c32 * 32 + c4;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+          const int jr = k * 4 + (lane >> 3);
+          const int64_t grow = rbase + jr;
+          if (grow < M && gcol < K)
+            *reinterpret_cast<float4*>(C + grow * ldc + gcol) = *reinterpret_cast<const float4*>(tile + jr * kPEpiStride + c4);
+        }
+        __syncwarp();
+      }
+      ptx::tc_fence_before_sync();
+      __syncwarp();
+      if (lane == 0) {
+        ptx::mbar_arrive(&sm.tempty[set]);
+        ptx::mbar_arrive(&sm.qempty[j % kPQ]);
+      }
+    }
+  }
+  ptx::tc_fence_before_sync();
+  __syncthreads();
+  if (warp == 1) {
+    ptx::tc_fence_after_sync();
+    ptx::tmem_dealloc(tmem, kPTmemCols);
+  }
+}
+
+template <typename BT>
+int launch_sddmm_persist_t(const BatchProblemTc* probs, const int4* items, int n_items, int* counter, int64_t N,
+                           cudaStream_t st) {
+  constexpr size_t smem = sizeof(SddmmSmem) + kPSmemAlign;
+  static bool configured[64] = {false};
+  int dev = 0;
+  BSP_CUDA(cudaGetDevice(&dev));
+  if (dev >= 64 || !configured[dev]) {
+    BSP_CUDA(cudaFuncSetAttribute(k_batched_sddmm_persist<BT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (dev < 64) configured[dev] = true;
+  }
+  BSP_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), st));
+  const int grid = std::min(num_sms(), n_items);
+  k_batched_sddmm_persist<BT><<<grid, kSdThreads, smem, st>>>(probs, items, n_items, counter, N);
+  BSP_LAUNCHED();
+  return BSP_OK;
+}
+
 }  // namespace
 
 
@@ -429,6 +666,8 @@ struct bsp_batch {
   bsp::BatchProblemTc* probs_s = nullptr;  // SDDMM (map = G, map2 = X)
   int4* items = nullptr;
   int4* items_s = nullptr;
+  int4* items_sp = nullptr;  // SDDMM items of the persistent kernel: (problem, 128 rows, 256 columns)
+  int n_items_sp = 0;
   int* counter = nullptr;  // next item of the persistent kernel (reset by every run)
   int shape = 0;           // persistent kernel's shape (bsp_batch_tune)
 };
@@ -437,12 +676,14 @@ namespace {
 
 // Uploads records and items into one device block and fills the batch.
 int batch_upload(bsp_batch* b, const std::vector<bsp::BatchProblemTc>& p1, const std::vector<int4>& i1,
-                 const std::vector<bsp::BatchProblemTc>& p2, const std::vector<int4>& i2, cudaStream_t s) {
+                 const std::vector<bsp::BatchProblemTc>& p2, const std::vector<int4>& i2, cudaStream_t s,
+                 const std::vector<int4>& i3 = {}) {
   using namespace bsp;
   auto up = [](size_t bytes) { return (std::max<size_t>(bytes, 1) + 255) & ~size_t(255); };
   const size_t o_p1 = 0, o_i1 = o_p1 + up(sizeof(BatchProblemTc) * p1.size());
   const size_t o_p2 = o_i1 + up(sizeof(int4) * i1.size()), o_i2 = o_p2 + up(sizeof(BatchProblemTc) * p2.size());
-  const size_t o_c = o_i2 + up(sizeof(int4) * i2.size()), total = o_c + 256;
+  const size_t o_i3 = o_i2 + up(sizeof(int4) * i2.size());
+  const size_t o_c = o_i3 + up(sizeof(int4) * i3.size()), total = o_c + 256;
   cudaError_t e = cudaMalloc(&b->dev, total);
   if (e != cudaSuccess) {
     cuda_status(e);
@@ -454,14 +695,17 @@ int batch_upload(bsp_batch* b, const std::vector<bsp::BatchProblemTc>& p1, const
   b->items = reinterpret_cast<int4*>(base + o_i1);
   b->probs_s = reinterpret_cast<BatchProblemTc*>(base + o_p2);
   b->items_s = reinterpret_cast<int4*>(base + o_i2);
+  b->items_sp = reinterpret_cast<int4*>(base + o_i3);
   b->counter = reinterpret_cast<int*>(base + o_c);
   b->n_items = (int)i1.size();
   b->n_items_s = (int)i2.size();
+  b->n_items_sp = (int)i3.size();
   struct Part { void* dst; const void* src; size_t bytes; };
-  const Part parts[4] = {{b->probs, p1.data(), sizeof(BatchProblemTc) * p1.size()},
+  const Part parts[5] = {{b->probs, p1.data(), sizeof(BatchProblemTc) * p1.size()},
                          {b->items, i1.data(), sizeof(int4) * i1.size()},
                          {b->probs_s, p2.data(), sizeof(BatchProblemTc) * p2.size()},
-                         {b->items_s, i2.data(), sizeof(int4) * i2.size()}};
+                         {b->items_s, i2.data(), sizeof(int4) * i2.size()},
+                         {b->items_sp, i3.data(), sizeof(int4) * i3.size()}};
   for (const Part& q : parts)
     if (q.bytes && (e = cudaMemcpyAsync(q.dst, q.src, q.bytes, cudaMemcpyHostToDevice, s)) != cudaSuccess)
       return cuda_status(e);
@@ -540,7 +784,7 @@ int bsp_batch_grad_create(const bsp_problem_grad* problems, int n, int64_t N, in
   if (dtype != BSP_BF16 && dtype != BSP_F16) return BSP_ERR_UNSUPPORTED;
   if (N % 8 != 0) return BSP_ERR_ALIGNMENT;
   std::vector<BatchProblemTc> pt, ps;
-  std::vector<int4> it, is;
+  std::vector<int4> it, is, isp;
   for (int i = 0; i < n; i++) {
     const bsp_problem_grad& p = problems[i];
     if (p.M < 0 || p.K < 0 || p.M > INT32_MAX || p.K > INT32_MAX) return BSP_ERR_INVALID_ARG;
@@ -579,6 +823,7 @@ int bsp_batch_grad_create(const bsp_problem_grad* problems, int n, int64_t N, in
       if (p.K > 0 && N > 0) {
         BSP_TRY(make_batch_map_sddmm(&r.map, p.G, dtype, p.M, N, p.ldg));
         BSP_TRY(make_batch_map_sddmm(&r.map2, p.X, dtype, p.K, N, p.ldx));
+        BSP_TRY(make_batch_map_sddmm(&r.map3, p.G, dtype, p.M, N, p.ldg, 128));
       }
       r.A = p.A_words;
       r.M = p.M;
@@ -591,9 +836,13 @@ int bsp_batch_grad_create(const bsp_problem_grad* problems, int n, int64_t N, in
       for (int64_t rb = 0; rb < ceil_div(p.M, kItemRows); rb++)
         for (int64_t kb = 0; kb < ceil_div(p.K, kItemCols); kb++)
           is.push_back(make_int4(idx, (int)rb, (int)kb, (int)ceil_div(N, 64)));
+      for (int64_t rb = 0; rb < ceil_div(p.M, (int64_t)kSdRows); rb++)
+        for (int64_t kb = 0; kb < ceil_div(p.K, (int64_t)kSdCols); kb++)
+          isp.push_back(make_int4(idx, (int)rb, (int)kb, (int)ceil_div(N, 64)));
     }
   }
-  if (it.size() > (size_t)INT32_MAX || is.size() > (size_t)INT32_MAX) return BSP_ERR_CAPACITY;
+  if (it.size() > (size_t)INT32_MAX || is.size() > (size_t)INT32_MAX || isp.size() > (size_t)INT32_MAX)
+    return BSP_ERR_CAPACITY;
   sort_items(it);
   sort_items(is);
   bsp_batch* b = new (std::nothrow) bsp_batch();
@@ -603,7 +852,7 @@ int bsp_batch_grad_create(const bsp_problem_grad* problems, int n, int64_t N, in
   b->bdt = dtype;
   b->grad = 1;
   cudaGetDevice(&b->device);
-  const int st = batch_upload(b, pt, it, ps, is, (cudaStream_t)stream);
+  const int st = batch_upload(b, pt, it, ps, is, (cudaStream_t)stream, isp);
   if (st != BSP_OK) {
     if (b->dev) cudaFree(b->dev);
     delete b;
@@ -696,6 +945,15 @@ int bsp_batched_spmm_grad(const bsp_batch* b, bsp_stream_t stream) {
   if (b->N == 0) return BSP_OK;
   const cudaStream_t s = (cudaStream_t)stream;
   BSP_TRY(launch_batched_tc(b->probs, b->items, b->n_items, b->N, b->bdt, s, 1));
+  // dA: the persistent SDDMM (BSP_BATCH_SDDMM_PERSIST=0 selects the CTA per
+  // 256x256 item, for comparisons)
+  const char* e = getenv("BSP_BATCH_SDDMM_PERSIST");
+  if (!(e && e[0] == '0')) {
+    if (b->n_items_sp == 0) return BSP_OK;
+    if (b->bdt == BSP_BF16)
+      return launch_sddmm_persist_t<__nv_bfloat16>(b->probs_s, b->items_sp, b->n_items_sp, b->counter, b->N, s);
+    return launch_sddmm_persist_t<__half>(b->probs_s, b->items_sp, b->n_items_sp, b->counter, b->N, s);
+  }
   return launch_batched_tc(b->probs_s, b->items_s, b->n_items_s, b->N, b->bdt, s, 2);
 }
 

@@ -957,8 +957,9 @@ int make_batch_map(CUtensorMap* m, const void* B, int bdt, int64_t K, int64_t N,
   return make_map(m, B, bdt, K, N, ldb, kBoxCols, kTcK, CU_TENSOR_MAP_SWIZZLE_128B);
 }
 
-int make_batch_map_sddmm(CUtensorMap* m, const void* T, int bdt, int64_t rows, int64_t N, int64_t ld) {
-  return make_map(m, T, bdt, rows, N, ld, kSdK, kCtaM, CU_TENSOR_MAP_SWIZZLE_128B);
+int make_batch_map_sddmm(CUtensorMap* m, const void* T, int bdt, int64_t rows, int64_t N, int64_t ld,
+                         int box_rows) {
+  return make_map(m, T, bdt, rows, N, ld, kSdK, (uint32_t)box_rows, CU_TENSOR_MAP_SWIZZLE_128B);
 }
 
 int launch_batched_tc(const BatchProblemTc* probs, const int4* items, int n_items, int64_t N, int bdt,

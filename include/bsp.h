@@ -299,19 +299,21 @@ typedef struct bsp_problem_grad {
 
 /* Prepare a gradient batch: n problems sharing N (multiple of 8) and the
  * 16-bit type of X and G.  Encodes the G and X tensor maps, uploads them
- * with two work lists — (problem, 256-row block of dX, 256-column block)
- * and (problem, 256-row block of dA, 256-column block of dA) — sorted
+ * with the work lists — (problem, 256-row block of dX, 256-column block)
+ * and (problem, 128-row block of dA, 256-column block of dA) — sorted
  * longest reduction first; synchronises the stream once.  Buffers are
  * referenced and must outlive the batch; bsp_batch_destroy releases it.
  * No reference counterpart (the reference has no backward pass); the
  * single-problem forms are bsp_spmm_t and bsp_sddmm.                      */
 int bsp_batch_grad_create(const bsp_problem_grad* problems, int n, int64_t N,
                           int dtype, bsp_batch** batch, bsp_stream_t stream);
-/* Every dX and dA of a gradient batch: two tensor-core launches (a CTA per
- * work item), no host synchronisation, no allocation.  dX sums every 32-row
- * tile of A (a batch has no occupancy plan); dA skips blocks of A without
- * set bits and writes them as zeros.  Runs of one batch must not overlap
- * on the GPU: they write the same dX and dA buffers.                       */
+/* Every dX and dA of a gradient batch: two tensor-core launches, no host
+ * synchronisation, no allocation.  dX (a CTA per work item) sums every
+ * 32-row tile of A (a batch has no occupancy plan); dA is one persistent
+ * launch (a CTA per SM taking items from a work queue in the batch's
+ * device memory, reset by a memset in the same stream) that writes zeros
+ * off A's set bits.  Runs of one batch must not overlap on the GPU: they
+ * share the queue and write the same dX and dA buffers.                    */
 int bsp_batched_spmm_grad(const bsp_batch* batch, bsp_stream_t stream);
 
 /* ======================================================================== */
