@@ -104,7 +104,7 @@ __device__ __forceinline__ bool warp_wait_read(uint64_t* bar, uint32_t parity, c
   return ok != 0;
 }
 
-template <typename BT, int STAGES, int EPIW, int WA>
+template <typename BT, int STAGES, int EPIW, int WA, bool TR>
 __global__ void __launch_bounds__((kPEpiWarp0 + EPIW) * 32, 1)
     k_batched_persist(const BatchProblemTc* __restrict__ probs, const int4* __restrict__ items, int n_items,
                       int* next_item, int64_t N) {
@@ -158,7 +158,16 @@ __global__ void __launch_bounds__((kPEpiWarp0 + EPIW) * 32, 1)
       const int64_t M = p->M, Kw = p->Kw;
       const int64_t arow = (int64_t)w4.y * kPRows + r;
       const int nt = w4.w, nst = (nt + kPTps - 1) / kPTps;
-      auto load_word = [&](int k) -> uint32_t { return (k < nt && arow < M) ? __ldg(A + arow * Kw + k) : 0u; };
+      // forward: word k (a 32-column K tile) of row arow; Aᵀ·G: the words of
+      // the item's 256 A columns in A rows 32k.. (thread r: row 32k + r % 32,
+      // word r / 32 of the block)
+      auto load_word = [&](int k) -> uint32_t {
+        if (k >= nt) return 0u;
+        if (!TR) return arow < M ? __ldg(A + arow * Kw + k) : 0u;
+        const int64_t ar = (int64_t)k * kPK + (r & 31);
+        const int64_t wc = (int64_t)w4.y * (kPRows / 32) + (r >> 5);
+        return (ar < M && wc < Kw) ? __ldg(A + ar * Kw + wc) : 0u;
+      };
       uint32_t wq[kPWordAhead][kPTps];
 #pragma unroll
       for (int a = 0; a < kPWordAhead; a++)
@@ -181,9 +190,17 @@ __global__ void __launch_bounds__((kPEpiWarp0 + EPIW) * 32, 1)
           if (kPTps * i + u >= nt) continue;
           uint4 e[4];
           tc::expand32_two(wq[0][u], e);
-          uint8_t* as = sm.a + s * kPAStage + u * kPATile + (r >> 3) * tc::kSbo + (r & 7) * 16;
+          uint8_t* at = sm.a + s * kPAStage + u * kPATile;
+          if (!TR) {  // row r of the tile: half r/128 at 8 KB, then core matrices
+            uint8_t* as = at + (r >> 3) * tc::kSbo + (r & 7) * 16;
 #pragma unroll
-          for (int c = 0; c < 4; c++) *reinterpret_cast<uint4*>(as + c * tc::kLbo) = e[c];
+            for (int c = 0; c < 4; c++) *reinterpret_cast<uint4*>(as + c * tc::kLbo) = e[c];
+          } else {  // A row j of the tile, word wk of the block: output rows wk*32 + 8c ..
+            const int j = r & 31, wk = r >> 5;
+            uint8_t* as = at + (j >> 3) * tc::kLbo + (j & 7) * 16;
+#pragma unroll
+            for (int c = 0; c < 4; c++) *reinterpret_cast<uint4*>(as + (wk * 4 + c) * tc::kSbo) = e[c];
+          }
         }
         ptx::fence_proxy_async_smem();
         __syncwarp();
@@ -240,7 +257,7 @@ __global__ void __launch_bounds__((kPEpiWarp0 + EPIW) * 32, 1)
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
       const uint32_t ab = std::is_same<BT, __nv_bfloat16>::value ? 1u : 0u;
-      const uint32_t idesc = tc::idesc_f16(ab, 0u, 1u, (uint32_t)(nbox * 64), kPM);
+      const uint32_t idesc = tc::idesc_f16(ab, TR ? 1u : 0u, 1u, (uint32_t)(nbox * 64), kPM);
       const uint64_t adesc = ptx::smem_desc_noswizzle_u32(ptx::smem_addr(sm.a), tc::kLbo, tc::kSbo);
       const uint64_t bdesc = ptx::smem_desc_noswizzle_u32(ptx::smem_addr(sm.b), kPBox, 1024) |
                              ((uint64_t)tc::kLayoutSw128 << 61);
@@ -253,8 +270,8 @@ __global__ void __launch_bounds__((kPEpiWarp0 + EPIW) * 32, 1)
         const int it = *(volatile const int*)&sm.qitem[j % kPQ];
         if (it < 0) break;
         const int4 w4 = __ldg(items + it);
-        const int64_t M = probs[w4.x].M;
-        const int halves = (int64_t)w4.y * kPRows + kPM < M ? 3 : 1;
+        const int64_t out_rows = TR ? probs[w4.x].K : probs[w4.x].M;  // rows of C (dX: A's columns)
+        const int halves = (int64_t)w4.y * kPRows + kPM < out_rows ? 3 : 1;
         const int nt = w4.w, nst = (nt + kPTps - 1) / kPTps;
         const int set = j & 1;
         if (j >= 2 && !ptx::mbar_wait(&sm.tempty[set], (uint32_t)((j >> 1) - 1) & 1u)) {
@@ -312,7 +329,7 @@ __global__ void __launch_bounds__((kPEpiWarp0 + EPIW) * 32, 1)
       if (it < 0) break;
       const int4 w4 = __ldg(items + it);
       const BatchProblemTc* p = probs + w4.x;
-      const int64_t M = p->M, ldc = p->ldc;
+      const int64_t M = TR ? p->K : p->M, ldc = p->ldc;  // rows of C (dX: A's columns)
       float* C = p->C;
       const int nt = w4.w;
       const int set = j & 1;
@@ -376,11 +393,11 @@ __global__ void __launch_bounds__((kPEpiWarp0 + EPIW) * 32, 1)
   }
 }
 
-template <typename BT, int STAGES, int EPIW, int WA>
+template <typename BT, int STAGES, int EPIW, int WA, bool TR>
 int launch_persist_s(const BatchProblemTc* probs, const int4* items, int n_items, int* counter, int64_t N,
                      cudaStream_t st) {
   constexpr size_t smem = sizeof(PersistSmem<STAGES, EPIW>) + kPSmemAlign;
-  auto kern = k_batched_persist<BT, STAGES, EPIW, WA>;
+  auto kern = k_batched_persist<BT, STAGES, EPIW, WA, TR>;
   static bool configured[64] = {false};
   int dev = 0;
   BSP_CUDA(cudaGetDevice(&dev));
@@ -400,14 +417,14 @@ int launch_persist_s(const BatchProblemTc* probs, const int4* items, int n_items
 // 128 set: 3/4/4 192.6 us, 3/8/4 196.8 (its 576 threads spill 44 bytes at
 // 96 registers), 3/8/8 198.9, 4/4/4 202.3, 4/4/8 206.8.
 constexpr int kPersistShapes = 4;
-template <typename BT>
+template <typename BT, bool TR = false>
 int launch_persist_t(const BatchProblemTc* probs, const int4* items, int n_items, int* counter, int64_t N,
                      int shape, cudaStream_t st) {
   switch (shape) {
-    case 1: return launch_persist_s<BT, 3, 8, 4>(probs, items, n_items, counter, N, st);
-    case 2: return launch_persist_s<BT, 4, 4, 4>(probs, items, n_items, counter, N, st);
-    case 3: return launch_persist_s<BT, 3, 4, 8>(probs, items, n_items, counter, N, st);
-    default: return launch_persist_s<BT, 3, 4, 4>(probs, items, n_items, counter, N, st);
+    case 1: return launch_persist_s<BT, 3, 8, 4, TR>(probs, items, n_items, counter, N, st);
+    case 2: return launch_persist_s<BT, 4, 4, 4, TR>(probs, items, n_items, counter, N, st);
+    case 3: return launch_persist_s<BT, 3, 4, 8, TR>(probs, items, n_items, counter, N, st);
+    default: return launch_persist_s<BT, 3, 4, 4, TR>(probs, items, n_items, counter, N, st);
   }
 }
 
@@ -944,7 +961,19 @@ int bsp_batched_spmm_grad(const bsp_batch* b, bsp_stream_t stream) {
   if (dev != b->device) return BSP_ERR_INVALID_ARG;
   if (b->N == 0) return BSP_OK;
   const cudaStream_t s = (cudaStream_t)stream;
-  BSP_TRY(launch_batched_tc(b->probs, b->items, b->n_items, b->N, b->bdt, s, 1));
+  // dX = Aᵀ·G: for N ≤ 128 the persistent kernel in its transposed form
+  // (BSP_BATCH_PERSIST=0 selects the CTA per item, for comparisons)
+  const char* ep = getenv("BSP_BATCH_PERSIST");
+  if (b->N <= kPMaxN && !(ep && ep[0] == '0')) {
+    if (b->n_items > 0) {
+      const int rc = b->bdt == BSP_BF16
+                         ? launch_persist_t<__nv_bfloat16, true>(b->probs, b->items, b->n_items, b->counter, b->N, 0, s)
+                         : launch_persist_t<__half, true>(b->probs, b->items, b->n_items, b->counter, b->N, 0, s);
+      BSP_TRY(rc);
+    }
+  } else {
+    BSP_TRY(launch_batched_tc(b->probs, b->items, b->n_items, b->N, b->bdt, s, 1));
+  }
   // dA: the persistent SDDMM (BSP_BATCH_SDDMM_PERSIST=0 selects the CTA per
   // 256x256 item, for comparisons)
   const char* e = getenv("BSP_BATCH_SDDMM_PERSIST");

@@ -308,8 +308,9 @@ typedef struct bsp_problem_grad {
 int bsp_batch_grad_create(const bsp_problem_grad* problems, int n, int64_t N,
                           int dtype, bsp_batch** batch, bsp_stream_t stream);
 /* Every dX and dA of a gradient batch: two tensor-core launches, no host
- * synchronisation, no allocation.  dX (a CTA per work item) sums every
- * 32-row tile of A (a batch has no occupancy plan); dA is one persistent
+ * synchronisation, no allocation.  dX (for N ≤ 128 one persistent launch,
+ * else a CTA per work item) sums every 32-row tile of A (a batch has no
+ * occupancy plan); dA is one persistent
  * launch (a CTA per SM taking items from a work queue in the batch's
  * device memory, reset by a memset in the same stream) that writes zeros
  * off A's set bits.  Runs of one batch must not overlap on the GPU: they
