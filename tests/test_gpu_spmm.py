@@ -437,3 +437,42 @@ def test_prototype_sum_forms(tmp_path, form):
     A, _, _ = W.clustered_bits(1024, 3000, n_proto=5, p_proto=0.08, p_flip=0.004, seed_proto=5, seed_rows=6)
     B = np.random.default_rng(7).integers(-8, 9, (3000, 520)).astype(np.float32)
     assert np.array_equal(np.load(out).astype(np.float64), O.spmm_f64(W.pack_bits(A), 3000, B))
+
+
+_SLOT_SCRIPT = r"""
+import sys, numpy as np, torch
+sys.path.insert(0, sys.argv[1])
+from bitwise_spgemm_gb300 import capi, ops
+from bitwise_spgemm_gb300 import workloads as W
+A, _, _ = W.clustered_bits(2048, 4096, n_proto=12, p_proto=0.05, p_flip=0.004, seed_proto=8, seed_rows=9)
+wd = torch.from_numpy(np.ascontiguousarray(W.pack_bits(A)).view(np.int32)).cuda()
+B = torch.from_numpy(np.random.default_rng(10).standard_normal((4096, 512), dtype=np.float32)).cuda()
+outs = []
+for _ in range(2):  # two plans of the same A: rows of equal delta count may take other slots
+    plan = ops.Plan(wd, 4096, mode=capi.PLAN_PROTO)
+    outs.append(ops.spmm(wd, 4096, B, plan=plan))
+torch.cuda.synchronize()
+assert capi.device_status() == 0
+assert torch.equal(outs[0], outs[1])
+np.save(sys.argv[2], outs[0].cpu().numpy())
+"""
+
+
+def test_row_slot_order_does_not_change_results(tmp_path):
+    """The row kernel's slot order (longest delta lists first, equal lengths
+    in any order) and the index-order walk through the list bounds
+    (BSP_SLOT_LISTS=0) give the same FP32 C bit for bit, and so do two plans
+    of the same A."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    outs = []
+    for flag in ("1", "0"):
+        out = tmp_path / ("C%s.npy" % flag)
+        env = dict(os.environ, BSP_SLOT_LISTS=flag)
+        r = subprocess.run([sys.executable, "-c", _SLOT_SCRIPT, root, str(out)], env=env, capture_output=True,
+                           text=True, timeout=600)
+        assert r.returncode == 0, r.stderr[-2000:]
+        outs.append(np.load(out))
+    assert np.array_equal(outs[0], outs[1])
