@@ -37,7 +37,7 @@ def _run(probs, N):
     return dev
 
 
-@pytest.mark.parametrize("N", [128, 200, 520])
+@pytest.mark.parametrize("N", [40, 64, 128, 200, 520])
 def test_batched_matches_oracle(N):
     probs = _problems(24, N, seed=N)
     dev = _run(probs, N)
@@ -147,7 +147,7 @@ def _grad_problems(n, N, seed, integer):
     return out
 
 
-@pytest.mark.parametrize("N,integer", [(128, True), (128, False), (264, False)])
+@pytest.mark.parametrize("N,integer", [(24, True), (64, False), (128, True), (128, False), (264, False)])
 def test_batched_grad_matches_oracle(N, integer):
     """dX = Aᵀ·G and dA = (G·Xᵀ) ⊙ A for a batch of uneven problems against
     the FP64 oracle (integer-valued X and G exactly, N(0,1) within the scaled
