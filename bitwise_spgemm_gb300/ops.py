@@ -434,8 +434,9 @@ class Batch:
         call("bsp_batched_spmm", self._h, _stream())
 
     def tune(self):
-        """Time the persistent kernel's shapes on this batch (runs it 16
-        times), keep the fastest for later runs; returns (shape, ms)."""
+        """Time the persistent kernel's shapes on this batch (runs it four
+        times per shape), keep the fastest for later runs; returns (shape,
+        ms)."""
         shape, ms = C.c_int(), C.c_float()
         call("bsp_batch_tune", self._h, _stream(), C.byref(shape), C.byref(ms))
         return shape.value, ms.value

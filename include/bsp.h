@@ -272,7 +272,8 @@ int bsp_batched_spmm(const bsp_batch* batch, bsp_stream_t stream);
  * words loaded ahead) on this batch — each once to warm up, then three runs
  * — keeps the fastest in the batch for later bsp_batched_spmm calls and
  * returns its index and ms per run.  It runs the batch (writes its C
- * buffers) 16 times and synchronises the stream.  Batches of N > 128 have
+ * buffers) four times per shape and synchronises the stream.  Batches of
+ * N > 128 have
  * one shape (index 0); a gradient batch is refused (BSP_ERR_INVALID_ARG).
  * On an error the batch keeps its previous shape.                         */
 int bsp_batch_tune(bsp_batch* batch, bsp_stream_t stream, int* shape, float* ms);
